@@ -1,0 +1,169 @@
+/*
+ * mhsw.h -- C ABI of the GB300 read-to-contig Smith-Waterman driver.
+ *
+ * It replaces MHM2's ADEPT GPU aligner behind klign (reference
+ * src/adept-sw/driver.hpp:14-57, src/adept-sw/driver.cpp:28-417) with results that
+ * are bit-exact against the reference's CPU aligner
+ * (StripedSmithWaterman::Aligner::Align with Filter(true, false, 0, 32767),
+ * src/ssw/ssw.cpp:431-469, as klign calls it at src/klign.cpp:257).
+ *
+ * Conventions
+ *   - Every call returns an int status (MHSW_OK == 0); nothing throws across the ABI.
+ *     mhsw_driver_last_error() gives the message of the last failure on a handle.
+ *   - Scores are passed the way klign passes them to the reference GPU driver
+ *     (src/klign.cpp:464-465): match positive, penalties negated (e.g. 1, -3, -5, -2).
+ *   - "A" is the sequence SSW treats as its reference (the outer loop of
+ *     sw_sse2_byte, src/ssw/ssw_core.cpp:296) and "B" the one it profiles (its query).
+ *     klign calls Align(contig, read, ...) (src/klign.cpp:257), so in klign's
+ *     orientation A = read and B = contig window.  Tie-breaks follow SSW's roles.
+ *   - A handle serialises its own calls; use one handle per host thread.
+ *   - Result arrays returned by mhsw_get_aln_results() are owned by the handle and stay
+ *     valid until the next mhsw_run_kernel_* call or mhsw_driver_destroy().
+ */
+#ifndef MHSW_H_
+#define MHSW_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define MHSW_OK 0
+#define MHSW_ERR_CUDA 1      /* a CUDA runtime call failed */
+#define MHSW_ERR_ARG 2       /* invalid argument */
+#define MHSW_ERR_STATE 3     /* call out of order (e.g. backwards before forwards) */
+#define MHSW_ERR_NOMEM 4     /* host or device allocation failed */
+#define MHSW_ERR_LIMIT 5     /* a sequence exceeds the engine limits (see mhsw_limits) */
+#define MHSW_ERR_NO_GPU 6    /* no CUDA device */
+#define MHSW_ERR_INTERNAL 7  /* internal consistency check failed */
+
+/* ---- orientation ----------------------------------------------------------- */
+/* klign (default): reads are SSW's ref (A), contigs its query (B); results map
+ * query_* <- read coordinates, ref_* <- contig coordinates (src/klign.cpp:369-376). */
+#define MHSW_ORIENT_KLIGN 0
+/* test/ssw-test.cpp: the driver's "contigs" argument is SSW's ref (A) and "reads"
+ * its query (B) (test/ssw-test.cpp:44-66 with translate_adept_to_ssw, :22-40). */
+#define MHSW_ORIENT_REF_IS_A 1
+
+/* ---- forms ----------------------------------------------------------------- */
+#define MHSW_FORM_PLAIN 0    /* one wavefront group per pair, input order */
+#define MHSW_FORM_BATCHED 1  /* length-bucketed, sorted, persistent work-stealing launch */
+
+typedef struct mhsw_driver mhsw_driver;
+
+/* Result views, as in adept_sw::AlignmentResults (src/adept-sw/driver.hpp:17-23),
+ * plus exact int32 copies (the short views saturate beyond 32767). */
+typedef struct {
+  int16_t *ref_begin, *query_begin, *ref_end, *query_end, *top_scores;
+  int32_t *ref_begin32, *query_begin32, *ref_end32, *query_end32, *top_scores32;
+  int32_t n;
+} mhsw_aln_results;
+
+/* Device-timed figures of the last mhsw_align_pairs / run_kernel_* call. */
+typedef struct {
+  double fwd_ms;      /* forward kernels (incl. int32 re-runs) */
+  double rev_ms;      /* begin (reverse) kernels */
+  double total_ms;    /* all device work of the call incl. copies */
+  double fwd_cells;   /* sum over pairs of len(A) * len(B) */
+  int64_t n_pairs;
+  int64_t n_overflow16;  /* pairs re-run in int32 */
+  int64_t n_rev_wide;    /* begin searches that used the wavefront path */
+  int64_t launches;      /* kernels launched by the call */
+} mhsw_timing;
+
+typedef struct {
+  int32_t max_b_len;       /* longest B (SSW query) the kernels accept */
+  int32_t max_coord;       /* coordinates and lengths must stay below this */
+  int32_t int16_ceiling;   /* default score ceiling of the packed int16 engine */
+} mhsw_limits_t;
+
+/* A batch as concatenated bytes with per-pair offsets and lengths.  Pointers are
+ * host or device pointers depending on the call. */
+typedef struct {
+  const char *a_seq;
+  const int64_t *a_off;
+  const int32_t *a_len;
+  const char *b_seq;
+  const int64_t *b_off;
+  const int32_t *b_len;
+  int64_t n;
+} mhsw_pairs;
+
+/* ---- free functions (src/adept-sw/driver.hpp:25-35, driver.cpp:28-77) ------- */
+/* get_num_node_gpus (driver.cpp:47-52): 0 when no device or the runtime fails. */
+int mhsw_get_num_node_gpus(int *count);
+/* get_tot_gpu_mem (driver.cpp:41-45): totalGlobalMem of device 0. */
+int mhsw_get_tot_gpu_mem(size_t *bytes);
+/* get_avail_gpu_mem_per_rank (driver.cpp:28-33): 0.8 * total / (tot_ranks / devices). */
+int mhsw_get_avail_gpu_mem_per_rank(int tot_ranks, int num_devices, size_t *bytes);
+/* get_device_name (driver.cpp:35-39): the PCI bus id string. */
+int mhsw_get_device_name(int device_id, char *buf, size_t buflen);
+/* initialize_gpu (driver.cpp:54-77): first-touch of pinned memory, timed. */
+int mhsw_initialize_gpu(double *seconds, int *device_count, size_t *total_mem);
+int mhsw_limits(mhsw_limits_t *out);
+
+/* ---- driver handle (adept_sw::GPUDriver, driver.hpp:37-55) ------------------ */
+int mhsw_driver_create(mhsw_driver **out);
+/* ~GPUDriver (driver.cpp:249-268). */
+void mhsw_driver_destroy(mhsw_driver *drv);
+const char *mhsw_driver_last_error(const mhsw_driver *drv);
+
+/* GPUDriver::init (driver.cpp:198-247): device = rank_me % device_count; scores
+ * as klign passes them (negated penalties).  rlen_limit only pre-sizes buffers;
+ * batches of any size and length (up to mhsw_limits) are accepted.
+ * *seconds (may be NULL) receives the time spent. */
+int mhsw_driver_init(mhsw_driver *drv, int rank_me, int rank_n, short match_score, short mismatch_score,
+                     short gap_opening_score, short gap_extending_score, int rlen_limit, double *seconds);
+/* SSW's ambiguity penalty (N against anything), negated like the others.  The
+ * reference GPU driver has no such parameter (ADEPT compares raw bytes,
+ * src/adept-sw/kernel.cpp:308); klign's CPU path passes ALN_AMBIGUITY_COST
+ * (src/klign.cpp:423-424).  Default: -1 (ALN_AMBIGUITY_COST in CMakeDefinitions.txt:117). */
+int mhsw_driver_set_ambiguity(mhsw_driver *drv, short ambiguity_score);
+int mhsw_driver_set_orientation(mhsw_driver *drv, int orientation);
+/* Form used by run_kernel_forwards (default MHSW_FORM_PLAIN). */
+int mhsw_driver_set_form(mhsw_driver *drv, int form);
+/* Debug knob: pairs whose score exceeds `ceiling` in the packed int16 engine are
+ * re-run in int32 (default and maximum: mhsw_limits().int16_ceiling). */
+int mhsw_driver_set_int16_ceiling(mhsw_driver *drv, int ceiling);
+/* The CUDA stream (cudaStream_t) the handle launches on. */
+int mhsw_driver_stream(mhsw_driver *drv, void **stream);
+
+/* GPUDriver::run_kernel_forwards (driver.cpp:281-375): copies the batch, launches
+ * the forward pass and the copy of the end coordinates and scores; returns without
+ * waiting.  reads[i]/contigs[i] are byte strings of read_lens[i]/contig_lens[i]
+ * bytes.  max_read_size / max_contig_size are accepted for signature parity and
+ * checked as upper bounds. */
+int mhsw_run_kernel_forwards(mhsw_driver *drv, const char *const *reads, const int32_t *read_lens,
+                             const char *const *contigs, const int32_t *contig_lens, int32_t n,
+                             uint32_t max_read_size, uint32_t max_contig_size);
+/* GPUDriver::run_kernel_backwards (driver.cpp:377-417): launches the begin pass for
+ * the batch of the preceding run_kernel_forwards (same arguments) and the copy of
+ * begins; returns without waiting.  Unlike the reference, no host-side reduction
+ * (get_new_min_length, driver.cpp:170-180) runs between the passes. */
+int mhsw_run_kernel_backwards(mhsw_driver *drv, const char *const *reads, const int32_t *read_lens,
+                              const char *const *contigs, const int32_t *contig_lens, int32_t n,
+                              uint32_t max_read_size, uint32_t max_contig_size);
+/* GPUDriver::kernel_is_done (driver.cpp:270-274): *done = 1 when the last
+ * run_kernel_* call has completed. */
+int mhsw_kernel_is_done(mhsw_driver *drv, int *done);
+/* GPUDriver::kernel_block (driver.cpp:276-279). */
+int mhsw_kernel_block(mhsw_driver *drv);
+/* GPUDriver::get_aln_results (driver.hpp:54). */
+int mhsw_get_aln_results(mhsw_driver *drv, mhsw_aln_results *out);
+
+/* ---- batch entry points (the batched form and the benchmarks) --------------- */
+/* Aligns a whole batch synchronously: forward + begin pass.  host_io != 0: the
+ * pairs and out5 are host pointers (copies are part of the call); host_io == 0:
+ * they are device pointers already resident on the handle's device.
+ * out5[5*i .. 5*i+4] = score, a_begin, a_end, b_begin, b_end (SSW ref = A,
+ * SSW query = B; score 0 gives -1, -1, 0, 0 as SSW does). */
+int mhsw_align_pairs(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form);
+int mhsw_last_timing(mhsw_driver *drv, mhsw_timing *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MHSW_H_ */

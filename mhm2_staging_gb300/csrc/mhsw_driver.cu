@@ -1,0 +1,848 @@
+// mhsw_driver.cu -- host driver and C ABI (include/mhsw.h).
+//
+// Re-creates the call surface of the reference's adept_sw::GPUDriver
+// (src/adept-sw/driver.hpp:14-57, driver.cpp:28-417) on top of the GB300 kernels.
+// Differences from the reference, all internal:
+//   * both passes stay on one stream; the end coordinates feed the begin pass on the
+//     device (no host reduction between passes, driver.cpp:170-180);
+//   * buffers grow with the batch (no fixed KLIGN_GPU_BLOCK_SIZE cap, driver.cpp:213-242);
+//   * sequences travel as raw bytes and are translated on the device with SSW's table.
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mhsw.h"
+#include "mhsw_batch.h"
+#include "mhsw_engine.cuh"
+#include "mhsw_launch.h"
+
+namespace {
+
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t cap = 0;
+  cudaError_t reserve(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(n + n / 8, 64);
+    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+template <class T>
+struct HBuf {
+  T *p = nullptr;
+  size_t cap = 0;
+  cudaError_t reserve(size_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(n + n / 8, 64);
+    cudaError_t e = cudaMallocHost(&p, want * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+constexpr int kInt16Ceiling = mhsw::V16::kBig - 1 - 64;  // leaves room for one match step
+
+}  // namespace
+
+struct mhsw_driver {
+  std::mutex mu;
+  std::string err;
+  bool inited = false;
+  int device = 0;
+  mhsw::Scoring sc{1, 1, 1, 1, 1};
+  int orientation = MHSW_ORIENT_KLIGN;
+  int form = MHSW_FORM_PLAIN;
+  int ceiling16 = kInt16Ceiling;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev_done = nullptr;
+  bool ev_live = false;
+  cudaEvent_t ev_t[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+
+  // device batch
+  DBuf<char> a_seq, b_seq;
+  DBuf<int64_t> a_off, b_off;
+  DBuf<int32_t> a_len, b_len;
+  DBuf<int32_t> r_score, r_aend, r_bend, r_abeg, r_bbeg;
+  DBuf<uint32_t> r_flag;
+  DBuf<int64_t> l_ovf, l_wide;
+  DBuf<int> l_counts;
+  DBuf<unsigned char> scratch;
+  DBuf<unsigned char> outv;  // 5 x int16 + 5 x int32 arrays
+  DBuf<int32_t> out5;
+  mhsw::BatchState batch;     // batched-form work buffers
+
+  // pinned host staging
+  HBuf<char> h_a, h_b;
+  HBuf<int64_t> h_aoff, h_boff;
+  HBuf<int32_t> h_alen, h_blen;
+  HBuf<unsigned char> h_outv;
+  HBuf<int> h_counts;
+
+  // drop-in protocol state
+  int64_t n_batch = 0;
+  int max_a = 0, max_b = 0;
+  bool fwd_issued = false;
+  bool rev_issued = false;
+  double fwd_cells = 0;
+  int64_t launches = 0;
+  mhsw_timing timing{};
+
+  int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda_fail(cudaError_t e, const char *what) {
+    return fail(MHSW_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+
+  ~mhsw_driver() {
+    if (inited) cudaSetDevice(device);
+    if (st) cudaStreamSynchronize(st);
+    a_seq.release();
+    b_seq.release();
+    a_off.release();
+    b_off.release();
+    a_len.release();
+    b_len.release();
+    r_score.release();
+    r_aend.release();
+    r_bend.release();
+    r_abeg.release();
+    r_bbeg.release();
+    r_flag.release();
+    l_ovf.release();
+    l_wide.release();
+    l_counts.release();
+    scratch.release();
+    outv.release();
+    out5.release();
+    batch.release();
+    h_a.release();
+    h_b.release();
+    h_aoff.release();
+    h_boff.release();
+    h_alen.release();
+    h_blen.release();
+    h_outv.release();
+    h_counts.release();
+    for (auto &e : ev_t)
+      if (e) cudaEventDestroy(e);
+    if (ev_done) cudaEventDestroy(ev_done);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+#define MHSW_CK(expr, what)                              \
+  do {                                                   \
+    cudaError_t _e = (expr);                             \
+    if (_e != cudaSuccess) return d->cuda_fail(_e, what); \
+  } while (0)
+
+namespace {
+
+// Device buffers for n pairs and the byte totals; result arrays; lists.
+int ensure_device(mhsw_driver *d, int64_t n, int64_t a_bytes, int64_t b_bytes) {
+  MHSW_CK(d->a_seq.reserve((size_t)a_bytes + 16), "cudaMalloc A");
+  MHSW_CK(d->b_seq.reserve((size_t)b_bytes + 16), "cudaMalloc B");
+  MHSW_CK(d->a_off.reserve((size_t)n + 1), "cudaMalloc offsets");
+  MHSW_CK(d->b_off.reserve((size_t)n + 1), "cudaMalloc offsets");
+  MHSW_CK(d->a_len.reserve((size_t)n + 1), "cudaMalloc lengths");
+  MHSW_CK(d->b_len.reserve((size_t)n + 1), "cudaMalloc lengths");
+  return MHSW_OK;
+}
+
+int ensure_results(mhsw_driver *d, int64_t n) {
+  MHSW_CK(d->r_score.reserve((size_t)n + 1), "cudaMalloc results");
+  MHSW_CK(d->r_aend.reserve((size_t)n + 1), "cudaMalloc results");
+  MHSW_CK(d->r_bend.reserve((size_t)n + 1), "cudaMalloc results");
+  MHSW_CK(d->r_abeg.reserve((size_t)n + 1), "cudaMalloc results");
+  MHSW_CK(d->r_bbeg.reserve((size_t)n + 1), "cudaMalloc results");
+  MHSW_CK(d->r_flag.reserve((size_t)n + 1), "cudaMalloc results");
+  MHSW_CK(d->l_ovf.reserve((size_t)n + 1), "cudaMalloc lists");
+  MHSW_CK(d->l_wide.reserve((size_t)n + 1), "cudaMalloc lists");
+  MHSW_CK(d->l_counts.reserve(4), "cudaMalloc lists");
+  return MHSW_OK;
+}
+
+mhsw::ResultSet result_set(mhsw_driver *d) {
+  mhsw::ResultSet rs;
+  rs.score = d->r_score.p;
+  rs.a_end = d->r_aend.p;
+  rs.b_end = d->r_bend.p;
+  rs.a_beg = d->r_abeg.p;
+  rs.b_beg = d->r_bbeg.p;
+  rs.flag = d->r_flag.p;
+  return rs;
+}
+
+mhsw::WorkLists work_lists(mhsw_driver *d, int64_t n) {
+  mhsw::WorkLists wl;
+  wl.ovf = d->l_ovf.p;
+  wl.wide = d->l_wide.p;
+  wl.ovf_count = d->l_counts.p;
+  wl.wide_count = d->l_counts.p + 1;
+  wl.cap = n;
+  return wl;
+}
+
+// Scratch for multi-strip A (rows longer than one wavefront strip).
+int ensure_scratch(mhsw_driver *d, int max_a, int max_b, mhsw::FwdConfig *c16, mhsw::FwdConfig *c32, size_t *bytes) {
+  size_t need16 = mhsw::forward_scratch_bytes(*c16, max_a, max_b, false);
+  // the int32 paths (re-runs, wide begins) use a smaller grid when strips are needed
+  c32->grid = std::min(c32->grid, 152 * 2);
+  size_t need32 = mhsw::forward_scratch_bytes(*c32, max_a, max_b, true);
+  size_t need = std::max(need16, need32);
+  if (need > 0) MHSW_CK(d->scratch.reserve(need), "cudaMalloc scratch");
+  *bytes = need > 0 ? d->scratch.cap : 0;
+  return MHSW_OK;
+}
+
+// Forward pass over the staged PairSet: int16 engine, then int32 re-runs of the pairs
+// whose score crossed the ceiling.  Device-side lists; no host synchronisation.
+int run_forward(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, bool persistent_grid) {
+  mhsw::FwdConfig c16, c32;
+  cudaError_t e = mhsw::plan_forward(d->device, max_a, max_b, false, &c16);
+  if (e != cudaSuccess) return d->fail(MHSW_ERR_LIMIT, "B length %d exceeds the kernel limit %d", max_b, mhsw::kMaxB);
+  e = mhsw::plan_forward(d->device, max_a, max_b, true, &c32);
+  if (e != cudaSuccess) return d->fail(MHSW_ERR_LIMIT, "B length %d exceeds the kernel limit %d", max_b, mhsw::kMaxB);
+  const bool strips16 = max_a > 2 * c16.K * c16.G;
+  if (!persistent_grid && !strips16) {
+    int64_t g = (ps.n + c16.groups_per_block - 1) / c16.groups_per_block;
+    c16.grid = (int)std::max<int64_t>(1, std::min<int64_t>(g, 1 << 30));
+  }
+  size_t scr_bytes = 0;
+  int rc = ensure_scratch(d, max_a, max_b, &c16, &c32, &scr_bytes);
+  if (rc) return rc;
+  mhsw::ResultSet rs = result_set(d);
+  mhsw::WorkLists wl = work_lists(d, ps.n);
+  MHSW_CK(mhsw::reset_lists(wl, d->st), "reset lists");
+  MHSW_CK(mhsw::launch_forward(c16, false, ps, rs, d->sc, nullptr, nullptr, d->ceiling16, d->scratch.p, wl, d->st),
+          "forward int16 launch");
+  MHSW_CK(mhsw::launch_forward(c32, true, ps, rs, d->sc, wl.ovf, wl.ovf_count, 0x7fffffff, d->scratch.p, wl, d->st),
+          "forward int32 launch");
+  d->launches += 3;
+  return MHSW_OK;
+}
+
+// Forward pass in either form; lists are reset first so both passes see fresh counters.
+int forward_any(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, int form) {
+  if (form != MHSW_FORM_BATCHED) return run_forward(d, ps, max_a, max_b, false);
+  mhsw::WorkLists wl = work_lists(d, ps.n);
+  MHSW_CK(mhsw::reset_lists(wl, d->st), "reset lists");
+  d->launches += 1;
+  if (mhsw::batched_forward(d->batch, d->device, ps, result_set(d), wl, d->sc, d->ceiling16, max_a, max_b, d->st,
+                            &d->launches))
+    return d->fail(MHSW_ERR_CUDA, "batched forward: %s", d->batch.err.c_str());
+  // int32 pass over the pairs the int16 engine could not hold
+  mhsw::FwdConfig c16, c32;
+  if (mhsw::plan_forward(d->device, max_a, max_b, false, &c16) != cudaSuccess ||
+      mhsw::plan_forward(d->device, max_a, max_b, true, &c32) != cudaSuccess)
+    return d->fail(MHSW_ERR_LIMIT, "B length %d exceeds the kernel limit %d", max_b, mhsw::kMaxB);
+  size_t sb = 0;
+  int rc = ensure_scratch(d, max_a, max_b, &c16, &c32, &sb);
+  if (rc) return rc;
+  MHSW_CK(mhsw::launch_forward(c32, true, ps, result_set(d), d->sc, wl.ovf, wl.ovf_count, 0x7fffffff, d->scratch.p,
+                               wl, d->st),
+          "forward int32 launch");
+  d->launches += 1;
+  return MHSW_OK;
+}
+
+int run_reverse(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b) {
+  mhsw::ResultSet rs = result_set(d);
+  mhsw::WorkLists wl = work_lists(d, ps.n);
+  MHSW_CK(mhsw::launch_reverse(d->device, ps, rs, d->sc, max_a, max_b, d->scratch.p,
+                               d->scratch.p ? d->scratch.cap : 0, wl, d->st),
+          "begin pass launch");
+  d->launches += 2;
+  return MHSW_OK;
+}
+
+// Output views on the device: [5 x int16 arrays][5 x int32 arrays], n each.
+int ensure_outviews(mhsw_driver *d, int64_t n, mhsw::OutViews *dv, mhsw::OutViews *hv) {
+  size_t bytes = (size_t)n * (5 * sizeof(int16_t) + 5 * sizeof(int32_t)) + 64;
+  MHSW_CK(d->outv.reserve(bytes), "cudaMalloc outputs");
+  MHSW_CK(d->h_outv.reserve(bytes), "cudaMallocHost outputs");
+  auto carve = [n](unsigned char *base, mhsw::OutViews *v) {
+    int16_t *s = reinterpret_cast<int16_t *>(base);
+    v->s_score = s;
+    v->s_ref_beg = s + n;
+    v->s_ref_end = s + 2 * n;
+    v->s_qry_beg = s + 3 * n;
+    v->s_qry_end = s + 4 * n;
+    size_t off = ((size_t)n * 5 * sizeof(int16_t) + 15) / 16 * 16;
+    int32_t *w = reinterpret_cast<int32_t *>(base + off);
+    v->w_score = w;
+    v->w_ref_beg = w + n;
+    v->w_ref_end = w + 2 * n;
+    v->w_qry_beg = w + 3 * n;
+    v->w_qry_end = w + 4 * n;
+  };
+  carve(d->outv.p, dv);
+  carve(d->h_outv.p, hv);
+  return MHSW_OK;
+}
+
+int check_scoring(mhsw_driver *d, const mhsw::Scoring &s) {
+  if (s.match < 0 || s.mismatch < 0 || s.ambiguity < 0 || s.gap_open < 1 || s.gap_extend < 1)
+    return d->fail(MHSW_ERR_ARG,
+                   "scores must be match >= 0 and mismatch/ambiguity <= 0, gap open/extend <= -1 (negated penalties)");
+  if (s.match > 127 || s.mismatch > 127 || s.ambiguity > 127 || s.gap_open > 127 || s.gap_extend > 127)
+    return d->fail(MHSW_ERR_ARG, "score magnitudes above 127 are not supported");
+  return MHSW_OK;
+}
+
+// Stage a drop-in batch (pointer arrays) into pinned memory and on to the device.
+int stage_strings(mhsw_driver *d, const char *const *reads, const int32_t *read_lens, const char *const *contigs,
+                  const int32_t *contig_lens, int32_t n) {
+  const bool a_is_read = d->orientation == MHSW_ORIENT_KLIGN;
+  const char *const *as = a_is_read ? reads : contigs;
+  const int32_t *al = a_is_read ? read_lens : contig_lens;
+  const char *const *bs = a_is_read ? contigs : reads;
+  const int32_t *bl = a_is_read ? contig_lens : read_lens;
+  int64_t ta = 0, tb = 0;
+  int ma = 0, mb = 0;
+  for (int32_t i = 0; i < n; i++) {
+    if (al[i] < 0 || bl[i] < 0) return d->fail(MHSW_ERR_ARG, "negative length at pair %d", i);
+    ta += al[i];
+    tb += bl[i];
+    ma = std::max(ma, (int)al[i]);
+    mb = std::max(mb, (int)bl[i]);
+  }
+  if (mb > mhsw::kMaxB) return d->fail(MHSW_ERR_LIMIT, "sequence of %d bytes exceeds the limit %d", mb, mhsw::kMaxB);
+  MHSW_CK(d->h_a.reserve((size_t)ta + 16), "cudaMallocHost");
+  MHSW_CK(d->h_b.reserve((size_t)tb + 16), "cudaMallocHost");
+  MHSW_CK(d->h_aoff.reserve((size_t)n + 1), "cudaMallocHost");
+  MHSW_CK(d->h_boff.reserve((size_t)n + 1), "cudaMallocHost");
+  MHSW_CK(d->h_alen.reserve((size_t)n + 1), "cudaMallocHost");
+  MHSW_CK(d->h_blen.reserve((size_t)n + 1), "cudaMallocHost");
+  int64_t oa = 0, ob = 0;
+  for (int32_t i = 0; i < n; i++) {
+    d->h_aoff.p[i] = oa;
+    d->h_boff.p[i] = ob;
+    d->h_alen.p[i] = al[i];
+    d->h_blen.p[i] = bl[i];
+    if (al[i]) memcpy(d->h_a.p + oa, as[i], (size_t)al[i]);
+    if (bl[i]) memcpy(d->h_b.p + ob, bs[i], (size_t)bl[i]);
+    oa += al[i];
+    ob += bl[i];
+  }
+  int rc = ensure_device(d, n, ta, tb);
+  if (rc) return rc;
+  rc = ensure_results(d, n);
+  if (rc) return rc;
+  MHSW_CK(cudaMemcpyAsync(d->a_seq.p, d->h_a.p, (size_t)ta, cudaMemcpyHostToDevice, d->st), "H2D");
+  MHSW_CK(cudaMemcpyAsync(d->b_seq.p, d->h_b.p, (size_t)tb, cudaMemcpyHostToDevice, d->st), "H2D");
+  MHSW_CK(cudaMemcpyAsync(d->a_off.p, d->h_aoff.p, sizeof(int64_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
+  MHSW_CK(cudaMemcpyAsync(d->b_off.p, d->h_boff.p, sizeof(int64_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
+  MHSW_CK(cudaMemcpyAsync(d->a_len.p, d->h_alen.p, sizeof(int32_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
+  MHSW_CK(cudaMemcpyAsync(d->b_len.p, d->h_blen.p, sizeof(int32_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
+  d->max_a = ma;
+  d->max_b = mb;
+  d->n_batch = n;
+  double cells = 0;
+  for (int32_t i = 0; i < n; i++) cells += (double)al[i] * (double)bl[i];
+  d->fwd_cells = cells;
+  return MHSW_OK;
+}
+
+mhsw::PairSet staged_pairs(mhsw_driver *d) {
+  mhsw::PairSet ps;
+  ps.a_seq = d->a_seq.p;
+  ps.a_off = d->a_off.p;
+  ps.a_len = d->a_len.p;
+  ps.b_seq = d->b_seq.p;
+  ps.b_off = d->b_off.p;
+  ps.b_len = d->b_len.p;
+  ps.n = d->n_batch;
+  return ps;
+}
+
+int ready(mhsw_driver *d) {
+  if (!d) return MHSW_ERR_ARG;
+  if (!d->inited) return d->fail(MHSW_ERR_STATE, "driver not initialised (call mhsw_driver_init)");
+  MHSW_CK(cudaSetDevice(d->device), "cudaSetDevice");
+  return MHSW_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.f;
+  return ms;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mhsw_get_num_node_gpus(int *count) {
+  if (!count) return MHSW_ERR_ARG;
+  int c = 0;
+  if (cudaGetDeviceCount(&c) != cudaSuccess) {
+    cudaGetLastError();
+    c = 0;
+  }
+  *count = c;
+  return MHSW_OK;
+}
+
+int mhsw_get_tot_gpu_mem(size_t *bytes) {
+  if (!bytes) return MHSW_ERR_ARG;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return MHSW_ERR_CUDA;
+  }
+  *bytes = prop.totalGlobalMem;
+  return MHSW_OK;
+}
+
+int mhsw_get_avail_gpu_mem_per_rank(int tot_ranks, int num_devices, size_t *bytes) {
+  if (!bytes) return MHSW_ERR_ARG;
+  *bytes = 0;
+  if (num_devices == 0) mhsw_get_num_node_gpus(&num_devices);
+  if (num_devices <= 0) return MHSW_OK;
+  int ranks_per_device = tot_ranks / num_devices;
+  if (ranks_per_device < 1) ranks_per_device = 1;
+  size_t tot = 0;
+  int rc = mhsw_get_tot_gpu_mem(&tot);
+  if (rc) return rc;
+  *bytes = (size_t)((double)tot * 0.8) / (size_t)ranks_per_device;
+  return MHSW_OK;
+}
+
+int mhsw_get_device_name(int device_id, char *buf, size_t buflen) {
+  if (!buf || buflen == 0) return MHSW_ERR_ARG;
+  cudaError_t e = cudaDeviceGetPCIBusId(buf, (int)buflen, device_id);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    buf[0] = 0;
+    return MHSW_ERR_CUDA;
+  }
+  return MHSW_OK;
+}
+
+int mhsw_initialize_gpu(double *seconds, int *device_count, size_t *total_mem) {
+  auto t0 = std::chrono::steady_clock::now();
+  int c = 0;
+  mhsw_get_num_node_gpus(&c);
+  size_t tot = 0;
+  if (c > 0) {
+    mhsw_get_tot_gpu_mem(&tot);
+    double *first_touch = nullptr;
+    if (cudaMallocHost(&first_touch, sizeof(double)) == cudaSuccess) cudaFreeHost(first_touch);
+  }
+  if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (device_count) *device_count = c;
+  if (total_mem) *total_mem = tot;
+  return c > 0 ? MHSW_OK : MHSW_ERR_NO_GPU;
+}
+
+int mhsw_limits(mhsw_limits_t *out) {
+  if (!out) return MHSW_ERR_ARG;
+  out->max_b_len = mhsw::kMaxB;
+  out->max_coord = 0xFFFFF;
+  out->int16_ceiling = kInt16Ceiling;
+  return MHSW_OK;
+}
+
+int mhsw_driver_create(mhsw_driver **out) {
+  if (!out) return MHSW_ERR_ARG;
+  *out = new (std::nothrow) mhsw_driver();
+  return *out ? MHSW_OK : MHSW_ERR_NOMEM;
+}
+
+void mhsw_driver_destroy(mhsw_driver *drv) { delete drv; }
+
+const char *mhsw_driver_last_error(const mhsw_driver *drv) { return drv ? drv->err.c_str() : "null driver"; }
+
+int mhsw_driver_init(mhsw_driver *d, int rank_me, int rank_n, short match_score, short mismatch_score,
+                     short gap_opening_score, short gap_extending_score, int rlen_limit, double *seconds) {
+  if (!d) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  auto t0 = std::chrono::steady_clock::now();
+  (void)rank_n;
+  mhsw::Scoring s{match_score, -mismatch_score, -gap_opening_score, -gap_extending_score, d->sc.ambiguity};
+  int rc = check_scoring(d, s);
+  if (rc) return rc;
+  int count = 0;
+  mhsw_get_num_node_gpus(&count);
+  if (count <= 0) return d->fail(MHSW_ERR_NO_GPU, "no CUDA device");
+  if (d->inited) return d->fail(MHSW_ERR_STATE, "driver already initialised");
+  d->device = (rank_me < 0 ? 0 : rank_me) % count;
+  MHSW_CK(cudaSetDevice(d->device), "cudaSetDevice");
+  MHSW_CK(cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking), "cudaStreamCreate");
+  MHSW_CK(cudaEventCreateWithFlags(&d->ev_done, cudaEventDisableTiming), "cudaEventCreate");
+  for (auto &e : d->ev_t) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
+  d->sc = s;
+  d->inited = true;
+  // Pre-size for a reference-sized block (KLIGN_GPU_BLOCK_SIZE = 20000 pairs).
+  if (rlen_limit > 0) {
+    const int64_t n = 20000;
+    int r2 = ensure_device(d, n, (int64_t)rlen_limit * n, (int64_t)2 * rlen_limit * n);
+    if (r2) return r2;
+    r2 = ensure_results(d, n);
+    if (r2) return r2;
+  }
+  if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return MHSW_OK;
+}
+
+int mhsw_driver_set_ambiguity(mhsw_driver *d, short ambiguity_score) {
+  if (!d) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  mhsw::Scoring s = d->sc;
+  s.ambiguity = -ambiguity_score;
+  if (!d->inited) {
+    // allow setting before init: validate the ambiguity alone
+    if (s.ambiguity < 0 || s.ambiguity > 127) return d->fail(MHSW_ERR_ARG, "ambiguity score must be in [-127, 0]");
+    d->sc.ambiguity = s.ambiguity;
+    return MHSW_OK;
+  }
+  int rc = check_scoring(d, s);
+  if (rc) return rc;
+  d->sc = s;
+  return MHSW_OK;
+}
+
+int mhsw_driver_set_orientation(mhsw_driver *d, int orientation) {
+  if (!d) return MHSW_ERR_ARG;
+  if (orientation != MHSW_ORIENT_KLIGN && orientation != MHSW_ORIENT_REF_IS_A)
+    return d->fail(MHSW_ERR_ARG, "unknown orientation %d", orientation);
+  std::lock_guard<std::mutex> lk(d->mu);
+  d->orientation = orientation;
+  return MHSW_OK;
+}
+
+int mhsw_driver_set_form(mhsw_driver *d, int form) {
+  if (!d) return MHSW_ERR_ARG;
+  if (form != MHSW_FORM_PLAIN && form != MHSW_FORM_BATCHED) return d->fail(MHSW_ERR_ARG, "unknown form %d", form);
+  std::lock_guard<std::mutex> lk(d->mu);
+  d->form = form;
+  return MHSW_OK;
+}
+
+int mhsw_driver_set_int16_ceiling(mhsw_driver *d, int ceiling) {
+  if (!d) return MHSW_ERR_ARG;
+  if (ceiling < 0 || ceiling > kInt16Ceiling)
+    return d->fail(MHSW_ERR_ARG, "ceiling must be in [0, %d]", kInt16Ceiling);
+  std::lock_guard<std::mutex> lk(d->mu);
+  d->ceiling16 = ceiling;
+  return MHSW_OK;
+}
+
+int mhsw_driver_stream(mhsw_driver *d, void **stream) {
+  if (!d || !stream) return MHSW_ERR_ARG;
+  if (!d->inited) return d->fail(MHSW_ERR_STATE, "driver not initialised");
+  *stream = (void *)d->st;
+  return MHSW_OK;
+}
+
+int mhsw_run_kernel_forwards(mhsw_driver *d, const char *const *reads, const int32_t *read_lens,
+                             const char *const *contigs, const int32_t *contig_lens, int32_t n,
+                             uint32_t max_read_size, uint32_t max_contig_size) {
+  int rc = ready(d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (n < 0 || (n > 0 && (!reads || !read_lens || !contigs || !contig_lens)))
+    return d->fail(MHSW_ERR_ARG, "bad batch arguments");
+  for (int32_t i = 0; i < n; i++)
+    if ((uint32_t)read_lens[i] > max_read_size || (uint32_t)contig_lens[i] > max_contig_size)
+      return d->fail(MHSW_ERR_ARG, "pair %d longer than max_read_size/max_contig_size", i);
+  if (d->ev_live) MHSW_CK(cudaEventSynchronize(d->ev_done), "wait previous batch");
+  d->ev_live = false;
+  d->fwd_issued = d->rev_issued = false;
+  d->launches = 0;
+  MHSW_CK(cudaEventRecord(d->ev_t[0], d->st), "event");
+  rc = stage_strings(d, reads, read_lens, contigs, contig_lens, n);
+  if (rc) return rc;
+  mhsw::PairSet ps = staged_pairs(d);
+  MHSW_CK(cudaEventRecord(d->ev_t[1], d->st), "event");
+  if (n > 0) {
+    rc = forward_any(d, ps, d->max_a, d->max_b, d->form);
+    if (rc) return rc;
+  }
+  MHSW_CK(cudaEventRecord(d->ev_t[2], d->st), "event");
+  mhsw::OutViews dv, hv;
+  rc = ensure_outviews(d, std::max<int64_t>(n, 1), &dv, &hv);
+  if (rc) return rc;
+  const bool a_is_query = d->orientation == MHSW_ORIENT_KLIGN;
+  if (n > 0) {
+    MHSW_CK(mhsw::launch_finalize(result_set(d), n, a_is_query, 1, dv, d->st), "finalize");
+    d->launches += 1;
+    int16_t *srcs[3] = {dv.s_score, dv.s_ref_end, dv.s_qry_end};
+    int16_t *dsts[3] = {hv.s_score, hv.s_ref_end, hv.s_qry_end};
+    for (int k = 0; k < 3; k++)
+      MHSW_CK(cudaMemcpyAsync(dsts[k], srcs[k], sizeof(int16_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
+    int32_t *wsrc[3] = {dv.w_score, dv.w_ref_end, dv.w_qry_end};
+    int32_t *wdst[3] = {hv.w_score, hv.w_ref_end, hv.w_qry_end};
+    for (int k = 0; k < 3; k++)
+      MHSW_CK(cudaMemcpyAsync(wdst[k], wsrc[k], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
+  }
+  MHSW_CK(cudaEventRecord(d->ev_t[3], d->st), "event");
+  MHSW_CK(cudaEventRecord(d->ev_done, d->st), "event");
+  d->ev_live = true;
+  d->fwd_issued = true;
+  return MHSW_OK;
+}
+
+int mhsw_run_kernel_backwards(mhsw_driver *d, const char *const *reads, const int32_t *read_lens,
+                              const char *const *contigs, const int32_t *contig_lens, int32_t n,
+                              uint32_t max_read_size, uint32_t max_contig_size) {
+  int rc = ready(d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(d->mu);
+  (void)reads;
+  (void)read_lens;
+  (void)contigs;
+  (void)contig_lens;
+  (void)max_read_size;
+  (void)max_contig_size;
+  if (!d->fwd_issued) return d->fail(MHSW_ERR_STATE, "run_kernel_backwards without a preceding run_kernel_forwards");
+  if ((int64_t)n != d->n_batch)
+    return d->fail(MHSW_ERR_ARG, "batch size %d differs from the forward batch (%lld)", n, (long long)d->n_batch);
+  mhsw::PairSet ps = staged_pairs(d);
+  MHSW_CK(cudaEventRecord(d->ev_t[4], d->st), "event");
+  if (n > 0) {
+    rc = run_reverse(d, ps, d->max_a, d->max_b);
+    if (rc) return rc;
+  }
+  mhsw::OutViews dv, hv;
+  rc = ensure_outviews(d, std::max<int64_t>(n, 1), &dv, &hv);
+  if (rc) return rc;
+  const bool a_is_query = d->orientation == MHSW_ORIENT_KLIGN;
+  if (n > 0) {
+    MHSW_CK(mhsw::launch_finalize(result_set(d), n, a_is_query, 2, dv, d->st), "finalize");
+    d->launches += 1;
+    int16_t *srcs[2] = {dv.s_ref_beg, dv.s_qry_beg};
+    int16_t *dsts[2] = {hv.s_ref_beg, hv.s_qry_beg};
+    for (int k = 0; k < 2; k++)
+      MHSW_CK(cudaMemcpyAsync(dsts[k], srcs[k], sizeof(int16_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
+    int32_t *wsrc[2] = {dv.w_ref_beg, dv.w_qry_beg};
+    int32_t *wdst[2] = {hv.w_ref_beg, hv.w_qry_beg};
+    for (int k = 0; k < 2; k++)
+      MHSW_CK(cudaMemcpyAsync(wdst[k], wsrc[k], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
+    MHSW_CK(cudaMemcpyAsync(d->h_counts.reserve(4) == cudaSuccess ? d->h_counts.p : nullptr, d->l_counts.p,
+                            2 * sizeof(int), cudaMemcpyDeviceToHost, d->st),
+            "D2H counters");
+  }
+  MHSW_CK(cudaEventRecord(d->ev_t[5], d->st), "event");
+  MHSW_CK(cudaEventRecord(d->ev_done, d->st), "event");
+  d->ev_live = true;
+  d->rev_issued = true;
+  return MHSW_OK;
+}
+
+int mhsw_kernel_is_done(mhsw_driver *d, int *done) {
+  if (!d || !done) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (!d->ev_live) {
+    *done = 1;
+    return MHSW_OK;
+  }
+  cudaError_t e = cudaEventQuery(d->ev_done);
+  if (e == cudaErrorNotReady) {
+    *done = 0;
+    return MHSW_OK;
+  }
+  if (e != cudaSuccess) return d->cuda_fail(e, "cudaEventQuery");
+  *done = 1;
+  return MHSW_OK;
+}
+
+int mhsw_kernel_block(mhsw_driver *d) {
+  if (!d) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (!d->ev_live) return MHSW_OK;
+  MHSW_CK(cudaEventSynchronize(d->ev_done), "cudaEventSynchronize");
+  if (d->rev_issued && d->n_batch > 0 && d->h_counts.p) {
+    // timing of the completed protocol round
+    d->timing.fwd_ms = elapsed(d->ev_t[1], d->ev_t[2]);
+    d->timing.rev_ms = elapsed(d->ev_t[4], d->ev_t[5]);
+    d->timing.total_ms = elapsed(d->ev_t[0], d->ev_t[5]);
+    d->timing.fwd_cells = d->fwd_cells;
+    d->timing.n_pairs = d->n_batch;
+    d->timing.n_overflow16 = d->h_counts.p[0];
+    d->timing.n_rev_wide = d->h_counts.p[1];
+    d->timing.launches = d->launches;
+  }
+  return MHSW_OK;
+}
+
+int mhsw_get_aln_results(mhsw_driver *d, mhsw_aln_results *out) {
+  if (!d || !out) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (!d->fwd_issued || !d->h_outv.p) return d->fail(MHSW_ERR_STATE, "no results yet");
+  mhsw::OutViews hv;
+  const int64_t n = std::max<int64_t>(d->n_batch, 1);
+  int16_t *s = reinterpret_cast<int16_t *>(d->h_outv.p);
+  hv.s_score = s;
+  hv.s_ref_beg = s + n;
+  hv.s_ref_end = s + 2 * n;
+  hv.s_qry_beg = s + 3 * n;
+  hv.s_qry_end = s + 4 * n;
+  size_t off = ((size_t)n * 5 * sizeof(int16_t) + 15) / 16 * 16;
+  int32_t *w = reinterpret_cast<int32_t *>(d->h_outv.p + off);
+  out->top_scores = hv.s_score;
+  out->ref_begin = hv.s_ref_beg;
+  out->ref_end = hv.s_ref_end;
+  out->query_begin = hv.s_qry_beg;
+  out->query_end = hv.s_qry_end;
+  out->top_scores32 = w;
+  out->ref_begin32 = w + n;
+  out->ref_end32 = w + 2 * n;
+  out->query_begin32 = w + 3 * n;
+  out->query_end32 = w + 4 * n;
+  out->n = (int32_t)d->n_batch;
+  return MHSW_OK;
+}
+
+int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form) {
+  int rc = ready(d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (!pairs || pairs->n < 0 || (pairs->n > 0 && !out5)) return d->fail(MHSW_ERR_ARG, "bad pairs");
+  if (form != MHSW_FORM_PLAIN && form != MHSW_FORM_BATCHED) return d->fail(MHSW_ERR_ARG, "unknown form %d", form);
+  if (d->ev_live) MHSW_CK(cudaEventSynchronize(d->ev_done), "wait previous batch");
+  d->ev_live = false;
+  d->fwd_issued = d->rev_issued = false;
+  const int64_t n = pairs->n;
+  d->launches = 0;
+  int ma = 0, mb = 0;
+  double cells = 0;
+  mhsw::PairSet ps;
+  MHSW_CK(cudaEventRecord(d->ev_t[0], d->st), "event");
+  if (host_io) {
+    int64_t ta = 0, tb = 0;
+    for (int64_t i = 0; i < n; i++) {
+      const int32_t la = pairs->a_len[i], lb = pairs->b_len[i];
+      if (la < 0 || lb < 0) return d->fail(MHSW_ERR_ARG, "negative length at pair %lld", (long long)i);
+      ma = std::max(ma, (int)la);
+      mb = std::max(mb, (int)lb);
+      ta = std::max(ta, pairs->a_off[i] + la);
+      tb = std::max(tb, pairs->b_off[i] + lb);
+      cells += (double)la * (double)lb;
+    }
+    rc = ensure_device(d, n, ta, tb);
+    if (rc) return rc;
+    MHSW_CK(cudaMemcpyAsync(d->a_seq.p, pairs->a_seq, (size_t)ta, cudaMemcpyHostToDevice, d->st), "H2D");
+    MHSW_CK(cudaMemcpyAsync(d->b_seq.p, pairs->b_seq, (size_t)tb, cudaMemcpyHostToDevice, d->st), "H2D");
+    MHSW_CK(cudaMemcpyAsync(d->a_off.p, pairs->a_off, sizeof(int64_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
+    MHSW_CK(cudaMemcpyAsync(d->b_off.p, pairs->b_off, sizeof(int64_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
+    MHSW_CK(cudaMemcpyAsync(d->a_len.p, pairs->a_len, sizeof(int32_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
+    MHSW_CK(cudaMemcpyAsync(d->b_len.p, pairs->b_len, sizeof(int32_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
+    ps.a_seq = d->a_seq.p;
+    ps.a_off = d->a_off.p;
+    ps.a_len = d->a_len.p;
+    ps.b_seq = d->b_seq.p;
+    ps.b_off = d->b_off.p;
+    ps.b_len = d->b_len.p;
+  } else {
+    // device-resident inputs: lengths are read back once to size the launch
+    std::vector<int32_t> la((size_t)n), lb((size_t)n);
+    if (n > 0) {
+      MHSW_CK(cudaMemcpyAsync(la.data(), pairs->a_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
+      MHSW_CK(cudaMemcpyAsync(lb.data(), pairs->b_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
+      MHSW_CK(cudaStreamSynchronize(d->st), "sync");
+    }
+    for (int64_t i = 0; i < n; i++) {
+      ma = std::max(ma, (int)la[(size_t)i]);
+      mb = std::max(mb, (int)lb[(size_t)i]);
+      cells += (double)la[(size_t)i] * (double)lb[(size_t)i];
+    }
+    ps.a_seq = pairs->a_seq;
+    ps.a_off = pairs->a_off;
+    ps.a_len = pairs->a_len;
+    ps.b_seq = pairs->b_seq;
+    ps.b_off = pairs->b_off;
+    ps.b_len = pairs->b_len;
+  }
+  ps.n = n;
+  if (mb > mhsw::kMaxB) return d->fail(MHSW_ERR_LIMIT, "sequence of %d bytes exceeds the limit %d", mb, mhsw::kMaxB);
+  rc = ensure_results(d, n);
+  if (rc) return rc;
+  MHSW_CK(cudaEventRecord(d->ev_t[1], d->st), "event");
+  if (n > 0) {
+    rc = forward_any(d, ps, ma, mb, form);
+    if (rc) return rc;
+  }
+  MHSW_CK(cudaEventRecord(d->ev_t[2], d->st), "event");
+  if (n > 0) {
+    rc = run_reverse(d, ps, ma, mb);
+    if (rc) return rc;
+  }
+  MHSW_CK(cudaEventRecord(d->ev_t[3], d->st), "event");
+  if (n > 0) {
+    if (host_io) {
+      MHSW_CK(d->out5.reserve((size_t)n * 5), "cudaMalloc out5");
+      MHSW_CK(mhsw::launch_pack5(result_set(d), n, d->out5.p, d->st), "pack5");
+      MHSW_CK(cudaMemcpyAsync(out5, d->out5.p, sizeof(int32_t) * 5 * n, cudaMemcpyDeviceToHost, d->st), "D2H");
+    } else {
+      MHSW_CK(mhsw::launch_pack5(result_set(d), n, out5, d->st), "pack5");
+    }
+    d->launches += 1;
+    MHSW_CK(d->h_counts.reserve(4), "cudaMallocHost");
+    MHSW_CK(cudaMemcpyAsync(d->h_counts.p, d->l_counts.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->st), "D2H");
+  }
+  MHSW_CK(cudaEventRecord(d->ev_t[4], d->st), "event");
+  MHSW_CK(cudaEventSynchronize(d->ev_t[4]), "sync");
+  // Surface any asynchronous kernel fault as an error status.
+  MHSW_CK(cudaGetLastError(), "kernel execution");
+  d->timing.fwd_ms = elapsed(d->ev_t[1], d->ev_t[2]);
+  d->timing.rev_ms = elapsed(d->ev_t[2], d->ev_t[3]);
+  d->timing.total_ms = elapsed(d->ev_t[0], d->ev_t[4]);
+  d->timing.fwd_cells = cells;
+  d->timing.n_pairs = n;
+  d->timing.n_overflow16 = n > 0 ? d->h_counts.p[0] : 0;
+  d->timing.n_rev_wide = n > 0 ? d->h_counts.p[1] : 0;
+  d->timing.launches = d->launches;
+  return MHSW_OK;
+}
+
+int mhsw_last_timing(mhsw_driver *d, mhsw_timing *out) {
+  if (!d || !out) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  *out = d->timing;
+  return MHSW_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,435 @@
+// mhsw_kernels.cu -- forward, begin and output kernels of the alignment path (sm_103a).
+//
+// Forward  : k_fwd<V16|V32, K, G>  -- the wavefront engine of mhsw_engine.cuh, one
+//            G-lane group per pair (the reference's one-block-per-pair
+//            sequence_dna_kernel, src/adept-sw/kernel.cpp:160-333, replaced).
+// Begin    : k_rev_banded          -- one thread per pair, banded DP on the reversed
+//            prefixes A[0..a_end], B[0..b_end] (the reference's reverse pass,
+//            src/ssw/ssw_core.cpp:1166-1178 and src/adept-sw/kernel.cpp:335-509).
+//            Exact: every cell holding the score lies on an alignment from the end
+//            cell whose total gap length g obeys g*min(gO,gE) <= (a_end+1)*match - score,
+//            so the band |j - i| <= g contains it and banding only lowers other cells.
+//            k_rev_wave runs the wavefront engine on the reversed box for the rare
+//            pairs whose band is wider than kBandMax.
+// Output   : k_finalize / k_pack5  -- orientation mapping into the caller's arrays.
+#include <algorithm>
+#include <cstdio>
+
+#include "mhsw_engine.cuh"
+#include "mhsw_launch.h"
+
+namespace mhsw {
+
+
+namespace {
+
+constexpr int kG = 16;  // lanes per pair in every forward instantiation
+
+__device__ __forceinline__ unsigned group_mask(int G) {
+  if (G == 32) return 0xffffffffu;
+  const int lane32 = threadIdx.x & 31;
+  return ((1u << G) - 1u) << ((lane32 / G) * G);
+}
+
+template <class VT, int K, int G>
+__global__ void __launch_bounds__(256) k_fwd(PairSet ps, ResultSet rs, Scoring sc, const int64_t *__restrict__ list,
+                                             const int *__restrict__ list_count, int ceiling,
+                                             typename VT::Pay *scratch, int scratch_stride, WorkLists wl, int pad,
+                                             int bcap) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lanes = blockDim.x;
+  const int gpb = lanes / G;
+  const int grp = threadIdx.x / G;
+  const int lane = threadIdx.x % G;
+  const unsigned gmask = group_mask(G);
+  constexpr size_t kProf = group_prof_bytes<VT, K, G>();
+  unsigned char *gbase = smem + (size_t)grp * (kProf + (size_t)bcap);
+  GroupSmem gs;
+  gs.prof = reinterpret_cast<uint32_t *>(gbase);
+  gs.prof_lanes = G;
+  gs.bcodes = gbase + kProf;
+  gs.pad = pad;
+  gs.bcap = bcap;
+  constexpr int RS = 2 * K * G;
+  constexpr bool kWide = (VT::kWordsPerT == 2);
+
+  int64_t total = ps.n;
+  if (list) {
+    total = (int64_t)(*list_count);
+    if (total > wl.cap) total = wl.cap;
+  }
+  const int64_t gid = (int64_t)blockIdx.x * gpb + grp;
+  const int64_t gstride = (int64_t)gridDim.x * gpb;
+  typename VT::Pay *bnd = scratch ? scratch + gid * (int64_t)scratch_stride : nullptr;
+
+  for (int64_t i = gid; i < total; i += gstride) {
+    const int64_t p = list ? list[i] : i;
+    const int M = ps.a_len[p], N = ps.b_len[p];
+    const bool too_long = (N > bcap - pad - 2 * G) || (M > RS && (bnd == nullptr || N > scratch_stride));
+    if (M <= 0 || N <= 0 || too_long) {
+      if (lane == 0) {
+        rs.score[p] = 0;
+        rs.a_end[p] = -1;
+        rs.b_end[p] = 0;
+        rs.flag[p] = too_long ? kFlagTooLong : 0u;
+      }
+      continue;
+    }
+    SeqView A{ps.a_seq + ps.a_off[p], 1, M};
+    SeqView B{ps.b_seq + ps.b_off[p], 1, N};
+    SweepOut so;
+    sweep_pair<VT, K, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so);
+    if (lane == 0) {
+      const int S = key_value(so.key);
+      if (!kWide && so.overflow) {
+        rs.flag[p] = kFlagOverflow16;
+        const int slot = atomicAdd(wl.ovf_count, 1);
+        if (slot < wl.cap) wl.ovf[slot] = p;
+        rs.score[p] = S;
+        rs.a_end[p] = -1;
+        rs.b_end[p] = 0;
+      } else {
+        rs.flag[p] = 0u;
+        rs.score[p] = S;
+        rs.a_end[p] = S > 0 ? key_row(so.key) : -1;
+        rs.b_end[p] = S > 0 ? key_col(so.key) : 0;
+      }
+    }
+  }
+}
+
+// One thread per pair: banded begin search (see file header).
+__global__ void __launch_bounds__(128) k_rev_banded(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl) {
+  constexpr int NEG = -(1 << 29);
+  const int gO = sc.gap_open, gE = sc.gap_extend;
+  const int gmin = gO < gE ? gO : gE;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < ps.n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int S = rs.score[p];
+    if (rs.flag[p] & kFlagTooLong) {
+      rs.a_beg[p] = -1;
+      rs.b_beg[p] = 0;
+      continue;
+    }
+    if (S <= 0) {
+      rs.a_beg[p] = -1;
+      rs.b_beg[p] = 0;
+      continue;
+    }
+    const int ie = rs.a_end[p], je = rs.b_end[p];
+    const int M2 = ie + 1, N2 = je + 1;
+    long long gbl = ((long long)M2 * sc.match - S) / (gmin > 0 ? gmin : 1);
+    if (gbl < 0) gbl = 0;
+    if (gbl > (long long)M2 + N2) gbl = (long long)M2 + N2;
+    const int gb = (int)gbl;
+    const int W = 2 * gb + 1;
+    if (W > kBandMax) {
+      rs.flag[p] |= kFlagRevWide;
+      const int slot = atomicAdd(wl.wide_count, 1);
+      if (slot < wl.cap) wl.wide[slot] = p;
+      continue;
+    }
+    int Harr[kBandMax + 1], Earr[kBandMax + 1];
+    for (int d = 0; d <= W; d++) {
+      Harr[d] = 0;
+      Earr[d] = NEG;
+    }
+    const char *a = ps.a_seq + ps.a_off[p];
+    const char *b = ps.b_seq + ps.b_off[p];
+    int best = 0, bi = -1, bj = 0;
+    for (int i = 0; i < M2; i++) {
+      const int ca = c_code[(unsigned char)a[ie - i]];
+      const int jlo = i - gb;
+      int F = NEG;
+      for (int d = 0; d < W; d++) {
+        const int j = jlo + d;
+        if (j >= N2) break;
+        if (j < 0) {
+          Harr[d] = 0;
+          Earr[d] = NEG;
+          F = -gO;
+          continue;
+        }
+        const int hdiag = Harr[d], hup = Harr[d + 1], eup = Earr[d + 1];
+        const int cb = c_code[(unsigned char)b[je - j]];
+        const int e = max(eup - gE, hup - gO);
+        int h = hdiag + sub_score(ca, cb, sc, 1 << 28);
+        h = max(h, e);
+        h = max(h, F);
+        h = max(h, 0);
+        Harr[d] = h;
+        Earr[d] = e;
+        F = max(F - gE, h - gO);
+        if (h > best) {
+          best = h;
+          bi = i;
+          bj = j;
+        }
+      }
+      if (best >= S) break;
+    }
+    if (best != S) {
+      rs.flag[p] |= kFlagTooLong;  // inconsistent; reported as an error by the driver
+      rs.a_beg[p] = -1;
+      rs.b_beg[p] = 0;
+      continue;
+    }
+    rs.a_beg[p] = ie - bi;
+    rs.b_beg[p] = je - bj;
+  }
+}
+
+// Wavefront begin search on the reversed box for the pairs listed in wl.wide.
+template <int K, int G>
+__global__ void __launch_bounds__(256) k_rev_wave(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl, V32::Pay *scratch,
+                                                  int scratch_stride, int pad, int bcap) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lanes = blockDim.x;
+  const int gpb = lanes / G;
+  const int grp = threadIdx.x / G;
+  const int lane = threadIdx.x % G;
+  const unsigned gmask = group_mask(G);
+  constexpr size_t kProf = group_prof_bytes<V32, K, G>();
+  unsigned char *gbase = smem + (size_t)grp * (kProf + (size_t)bcap);
+  GroupSmem gs;
+  gs.prof = reinterpret_cast<uint32_t *>(gbase);
+  gs.prof_lanes = G;
+  gs.bcodes = gbase + kProf;
+  gs.pad = pad;
+  gs.bcap = bcap;
+  constexpr int RS = 2 * K * G;
+  const int gmin = sc.gap_open < sc.gap_extend ? sc.gap_open : sc.gap_extend;
+  const int64_t total = *wl.wide_count < wl.cap ? *wl.wide_count : wl.cap;
+  const int64_t gid = (int64_t)blockIdx.x * gpb + grp;
+  const int64_t gstride = (int64_t)gridDim.x * gpb;
+  V32::Pay *bnd = scratch ? scratch + gid * (int64_t)scratch_stride : nullptr;
+  for (int64_t i = gid; i < total; i += gstride) {
+    const int64_t p = wl.wide[i];
+    const int S = rs.score[p];
+    const int ie = rs.a_end[p], je = rs.b_end[p];
+    const int M2 = ie + 1;
+    long long gbl = ((long long)M2 * sc.match - S) / (gmin > 0 ? gmin : 1);
+    if (gbl < 0) gbl = 0;
+    long long n2 = (long long)M2 + gbl + 1;
+    if (n2 > je + 1) n2 = je + 1;
+    const int N2 = (int)n2;
+    const bool too_long = (N2 > bcap - pad - 2 * G) || (M2 > RS && (bnd == nullptr || N2 > scratch_stride));
+    if (too_long) {
+      if (lane == 0) {
+        rs.flag[p] |= kFlagTooLong;
+        rs.a_beg[p] = -1;
+        rs.b_beg[p] = 0;
+      }
+      continue;
+    }
+    SeqView A{ps.a_seq + ps.a_off[p] + ie, -1, M2};
+    SeqView B{ps.b_seq + ps.b_off[p] + je, -1, N2};
+    SweepOut so;
+    sweep_pair<V32, K, G>(A, B, sc, gs, lane, gmask, bnd, 0x7fffffff, so);
+    if (lane == 0) {
+      if (key_value(so.key) != S) {
+        rs.flag[p] |= kFlagTooLong;
+        rs.a_beg[p] = -1;
+        rs.b_beg[p] = 0;
+      } else {
+        rs.a_beg[p] = ie - key_row(so.key);
+        rs.b_beg[p] = je - key_col(so.key);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ int16_t to_short(int v) {
+  return (int16_t)(v > 32767 ? 32767 : (v < -32768 ? -32768 : v));
+}
+
+__global__ void k_finalize(ResultSet rs, int64_t n, bool a_is_query, int part, OutViews ov) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    if (part & 1) {
+      const int sc = rs.score[p], ae = rs.a_end[p], be = rs.b_end[p];
+      const int re = a_is_query ? be : ae, qe = a_is_query ? ae : be;
+      if (ov.s_score) ov.s_score[p] = to_short(sc);
+      if (ov.s_ref_end) ov.s_ref_end[p] = to_short(re);
+      if (ov.s_qry_end) ov.s_qry_end[p] = to_short(qe);
+      if (ov.w_score) ov.w_score[p] = sc;
+      if (ov.w_ref_end) ov.w_ref_end[p] = re;
+      if (ov.w_qry_end) ov.w_qry_end[p] = qe;
+    }
+    if (part & 2) {
+      const int ab = rs.a_beg[p], bb = rs.b_beg[p];
+      const int rb = a_is_query ? bb : ab, qb = a_is_query ? ab : bb;
+      if (ov.s_ref_beg) ov.s_ref_beg[p] = to_short(rb);
+      if (ov.s_qry_beg) ov.s_qry_beg[p] = to_short(qb);
+      if (ov.w_ref_beg) ov.w_ref_beg[p] = rb;
+      if (ov.w_qry_beg) ov.w_qry_beg[p] = qb;
+    }
+  }
+}
+
+__global__ void k_pack5(ResultSet rs, int64_t n, int32_t *out5) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    int32_t *o = out5 + 5 * p;
+    o[0] = rs.score[p];
+    o[1] = rs.a_beg[p];
+    o[2] = rs.a_end[p];
+    o[3] = rs.b_beg[p];
+    o[4] = rs.b_end[p];
+  }
+}
+
+__global__ void k_reset_lists(WorkLists wl) {
+  *wl.ovf_count = 0;
+  *wl.wide_count = 0;
+}
+
+int g_num_sms = 0;
+
+int num_sms(int device) {
+  if (g_num_sms == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
+    g_num_sms = v > 0 ? v : 1;
+  }
+  return g_num_sms;
+}
+
+size_t group_prof_rt(bool wide32, int K) {
+  if (wide32) return group_prof_bytes<V32, 4, kG>();
+  switch (K) {
+    case 2: return group_prof_bytes<V16, 2, kG>();
+    case 3: return group_prof_bytes<V16, 3, kG>();
+    case 4: return group_prof_bytes<V16, 4, kG>();
+    case 5: return group_prof_bytes<V16, 5, kG>();
+    case 6: return group_prof_bytes<V16, 6, kG>();
+    default: return group_prof_bytes<V16, 8, kG>();
+  }
+}
+
+template <class VT, int K>
+cudaError_t launch_fwd_t(const FwdConfig &cfg, const PairSet &ps, const ResultSet &rs, const Scoring &sc,
+                         const int64_t *list, const int *list_count, int ceiling, void *scratch, int scratch_stride,
+                         const WorkLists &wl, cudaStream_t st) {
+  auto kern = k_fwd<VT, K, kG>;
+  if (cfg.smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<cfg.grid, cfg.groups_per_block * kG, cfg.smem, st>>>(
+      ps, rs, sc, list, list_count, ceiling, reinterpret_cast<typename VT::Pay *>(scratch), scratch_stride, wl, cfg.pad,
+      cfg.bcap);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg) {
+  FwdConfig c{};
+  c.G = kG;
+  if (wide32) {
+    c.K = 4;
+  } else {
+    const int need = (max_a + 2 * kG - 1) / (2 * kG);  // K with 2*K*G >= max_a
+    if (need <= 2) c.K = 2;
+    else if (need <= 3) c.K = 3;
+    else if (need <= 4) c.K = 4;
+    else if (need <= 5) c.K = 5;
+    else if (need <= 6) c.K = 6;
+    else c.K = 8;
+  }
+  c.pad = 2 * kG;
+  if (max_b < 1) max_b = 1;
+  if (max_b > kMaxB) return cudaErrorInvalidValue;
+  c.bcap = ((c.pad + max_b + 2 * kG) + 15) / 16 * 16;
+  const size_t budget = 100 * 1024;  // keep two blocks per SM possible
+  const size_t per_group = group_prof_rt(wide32, c.K) + (size_t)c.bcap;
+  int gpb = 8;
+  while (gpb > 1 && (size_t)gpb * per_group > budget) gpb /= 2;
+  c.groups_per_block = gpb;
+  c.smem = (size_t)gpb * per_group;
+  if (c.smem > 220 * 1024) return cudaErrorInvalidValue;
+  int sms = num_sms(device);
+  c.grid = sms * 8;  // grid-stride; callers may lower it
+  *cfg = c;
+  return cudaSuccess;
+}
+
+size_t forward_scratch_bytes(const FwdConfig &cfg, int max_a, int max_b, bool wide32) {
+  const int RS = 2 * cfg.K * cfg.G;
+  if (max_a <= RS) return 0;
+  (void)max_b;
+  const size_t pay = wide32 ? sizeof(V32::Pay) : sizeof(V16::Pay);
+  return (size_t)cfg.grid * cfg.groups_per_block * (size_t)cfg.bcap * pay;  // stride = bcap payloads per group
+}
+
+cudaError_t launch_forward(const FwdConfig &cfg, bool wide32, const PairSet &ps, const ResultSet &rs,
+                           const Scoring &sc, const int64_t *list, const int *list_count, int ceiling,
+                           void *scratch, const WorkLists &wl, cudaStream_t st) {
+  // scratch stride (payloads per group) = B capacity
+  const int stride = cfg.bcap;
+  if (wide32) return launch_fwd_t<V32, 4>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
+  switch (cfg.K) {
+    case 2: return launch_fwd_t<V16, 2>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
+    case 3: return launch_fwd_t<V16, 3>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
+    case 4: return launch_fwd_t<V16, 4>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
+    case 5: return launch_fwd_t<V16, 5>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
+    case 6: return launch_fwd_t<V16, 6>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
+    default: return launch_fwd_t<V16, 8>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
+  }
+}
+
+cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, const Scoring &sc, int max_a,
+                           int max_b, void *scratch, size_t scratch_bytes, const WorkLists &wl, cudaStream_t st) {
+  if (ps.n > 0) {
+    int sms = num_sms(device);
+    int64_t blocks = (ps.n + 127) / 128;
+    int grid = (int)std::min<int64_t>(blocks, (int64_t)sms * 16);
+    k_rev_banded<<<grid, 128, 0, st>>>(ps, rs, sc, wl);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  // Wide bands: wavefront on the reversed box (count read on the device).
+  FwdConfig c;
+  cudaError_t e = plan_forward(device, max_a, max_b, true, &c);
+  if (e != cudaSuccess) return e;
+  const int RS = 2 * c.K * c.G;
+  int stride = c.bcap;
+  V32::Pay *scr = nullptr;
+  if (max_a > RS) {
+    // reuse the caller's scratch if it is large enough for a reduced grid
+    size_t per_group = (size_t)stride * sizeof(V32::Pay);
+    int groups = scratch ? (int)std::min<size_t>(scratch_bytes / per_group, (size_t)c.grid * c.groups_per_block) : 0;
+    if (groups >= c.groups_per_block) {
+      c.grid = groups / c.groups_per_block;
+      scr = reinterpret_cast<V32::Pay *>(scratch);
+    }
+  }
+  c.grid = std::max(1, std::min(c.grid, num_sms(device) * 4));
+  auto kern = k_rev_wave<4, kG>;
+  if (c.smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<c.grid, c.groups_per_block * kG, c.smem, st>>>(ps, rs, sc, wl, scr, stride, c.pad, c.bcap);
+  return cudaGetLastError();
+}
+
+cudaError_t reset_lists(const WorkLists &wl, cudaStream_t st) {
+  k_reset_lists<<<1, 1, 0, st>>>(wl);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const ResultSet &rs, int64_t n, bool a_is_query, int part, const OutViews &ov,
+                            cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  int grid = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  k_finalize<<<grid, 256, 0, st>>>(rs, n, a_is_query, part, ov);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack5(const ResultSet &rs, int64_t n, int32_t *out5, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  int grid = (int)std::min<int64_t>((n + 255) / 256, 4096);
+  k_pack5<<<grid, 256, 0, st>>>(rs, n, out5);
+  return cudaGetLastError();
+}
+
+}  // namespace mhsw

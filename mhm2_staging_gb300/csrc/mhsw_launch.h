@@ -1,0 +1,72 @@
+// mhsw_launch.h -- host-side launch entry points of the alignment kernels (internal).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mhsw {
+
+struct Scoring;
+struct PairSet;
+struct ResultSet;
+
+// Work lists built on the device (no host round trip between passes).
+struct WorkLists {
+  int64_t *ovf;       // pairs whose int16 forward pass crossed the ceiling
+  int *ovf_count;
+  int64_t *wide;      // pairs whose reverse band is wider than the banded kernel handles
+  int *wide_count;
+  int64_t cap;        // capacity of each list
+};
+
+struct FwdConfig {
+  int K;              // packed cell pairs per lane (rows per lane = 2K)
+  int G;              // lanes per pair
+  int groups_per_block;
+  int bcap;           // per-group B code buffer bytes (>= pad + maxB + 2G)
+  int pad;            // leading PAD entries
+  int grid;           // blocks (grid-stride over pairs)
+  size_t smem;        // dynamic shared memory bytes
+};
+
+// Upper bound of B length the forward kernels accept (shared-memory code buffer).
+constexpr int kMaxB = 65536;
+// Widest reverse band handled by the banded begin kernel; wider ones use the wavefront.
+constexpr int kBandMax = 256;
+
+// Chooses K/G/grid/smem for a forward launch over pairs whose A (rows) lengths are at
+// most max_a and B lengths at most max_b.  wide32 selects the int32 engine.
+cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg);
+
+// Bytes of strip scratch a forward launch needs (0 when A fits one strip).
+size_t forward_scratch_bytes(const FwdConfig &cfg, int max_a, int max_b, bool wide32);
+
+// Forward pass (int16, or int32 when wide32) over pairs [0, n) or over the device list
+// (list != nullptr, count read on the device).  Writes score, a_end, b_end, flag.
+cudaError_t launch_forward(const FwdConfig &cfg, bool wide32, const PairSet &ps, const ResultSet &rs,
+                           const Scoring &sc, const int64_t *list, const int *list_count, int ceiling,
+                           void *scratch, const WorkLists &wl, cudaStream_t st);
+
+// Begin pass: banded thread-per-pair kernel for all pairs, then the wavefront kernel on
+// reversed prefixes for the pairs listed in wl.wide.
+cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, const Scoring &sc, int max_a,
+                           int max_b, void *scratch, size_t scratch_bytes, const WorkLists &wl, cudaStream_t st);
+
+// Clears the device work-list counters.
+cudaError_t reset_lists(const WorkLists &wl, cudaStream_t st);
+
+// Output views in the caller's orientation (see mhsw.h).  out_* may be null.
+struct OutViews {
+  int16_t *s_score, *s_ref_beg, *s_ref_end, *s_qry_beg, *s_qry_end;
+  int32_t *w_score, *w_ref_beg, *w_ref_end, *w_qry_beg, *w_qry_end;
+};
+// a_is_query: A (SSW ref) is the caller's query (klign: reads); else A is the caller's ref.
+// part: 1 = ends + score, 2 = begins, 3 = all.
+cudaError_t launch_finalize(const ResultSet &rs, int64_t n, bool a_is_query, int part, const OutViews &ov,
+                            cudaStream_t st);
+
+// Packs results into n x 5 int32 rows (score, a_beg, a_end, b_beg, b_end).
+cudaError_t launch_pack5(const ResultSet &rs, int64_t n, int32_t *out5, cudaStream_t st);
+
+int launches_per_batch();
+
+}  // namespace mhsw

@@ -1,0 +1,391 @@
+"""Python mirror of the reference's GPU aligner surface, bound to libmhsw.so via ctypes.
+
+`GPUDriver` mirrors adept_sw::GPUDriver (reference src/adept-sw/driver.hpp:37-55):
+init / run_kernel_forwards / run_kernel_backwards / kernel_is_done / kernel_block /
+get_aln_results, with the same argument meaning (scores passed negated, reads then
+contigs) and the same error behaviour (a failed call raises RuntimeError, as the
+reference's cudaErrchk throws std::runtime_error, driver.cpp:17-26).
+
+There is no CPU fallback: if libmhsw.so is missing or no GPU is present the calls
+raise.  The CPU oracle lives in oracle/ and is only used by tests and benchmarks.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+from . import build as _build
+
+ORIENT_KLIGN = 0
+ORIENT_REF_IS_A = 1
+FORM_PLAIN = 0
+FORM_BATCHED = 1
+
+_P = C.c_void_p
+
+
+class _AlnResults(C.Structure):
+    _fields_ = [
+        ("ref_begin", C.POINTER(C.c_int16)),
+        ("query_begin", C.POINTER(C.c_int16)),
+        ("ref_end", C.POINTER(C.c_int16)),
+        ("query_end", C.POINTER(C.c_int16)),
+        ("top_scores", C.POINTER(C.c_int16)),
+        ("ref_begin32", C.POINTER(C.c_int32)),
+        ("query_begin32", C.POINTER(C.c_int32)),
+        ("ref_end32", C.POINTER(C.c_int32)),
+        ("query_end32", C.POINTER(C.c_int32)),
+        ("top_scores32", C.POINTER(C.c_int32)),
+        ("n", C.c_int32),
+    ]
+
+
+class Timing(C.Structure):
+    _fields_ = [
+        ("fwd_ms", C.c_double),
+        ("rev_ms", C.c_double),
+        ("total_ms", C.c_double),
+        ("fwd_cells", C.c_double),
+        ("n_pairs", C.c_int64),
+        ("n_overflow16", C.c_int64),
+        ("n_rev_wide", C.c_int64),
+        ("launches", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Limits(C.Structure):
+    _fields_ = [("max_b_len", C.c_int32), ("max_coord", C.c_int32), ("int16_ceiling", C.c_int32)]
+
+
+class PairsT(C.Structure):
+    _fields_ = [
+        ("a_seq", _P),
+        ("a_off", _P),
+        ("a_len", _P),
+        ("b_seq", _P),
+        ("b_off", _P),
+        ("b_len", _P),
+        ("n", C.c_int64),
+    ]
+
+
+# Every symbol include/mhsw.h declares, with its ctypes signature.
+SIGNATURES: dict[str, tuple] = {
+    "mhsw_get_num_node_gpus": (C.c_int, [C.POINTER(C.c_int)]),
+    "mhsw_get_tot_gpu_mem": (C.c_int, [C.POINTER(C.c_size_t)]),
+    "mhsw_get_avail_gpu_mem_per_rank": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_size_t)]),
+    "mhsw_get_device_name": (C.c_int, [C.c_int, C.c_char_p, C.c_size_t]),
+    "mhsw_initialize_gpu": (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_size_t)]),
+    "mhsw_limits": (C.c_int, [C.POINTER(Limits)]),
+    "mhsw_driver_create": (C.c_int, [C.POINTER(_P)]),
+    "mhsw_driver_destroy": (None, [_P]),
+    "mhsw_driver_last_error": (C.c_char_p, [_P]),
+    "mhsw_driver_init": (
+        C.c_int,
+        [_P, C.c_int, C.c_int, C.c_short, C.c_short, C.c_short, C.c_short, C.c_int, C.POINTER(C.c_double)],
+    ),
+    "mhsw_driver_set_ambiguity": (C.c_int, [_P, C.c_short]),
+    "mhsw_driver_set_orientation": (C.c_int, [_P, C.c_int]),
+    "mhsw_driver_set_form": (C.c_int, [_P, C.c_int]),
+    "mhsw_driver_set_int16_ceiling": (C.c_int, [_P, C.c_int]),
+    "mhsw_driver_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "mhsw_run_kernel_forwards": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32, C.c_uint32, C.c_uint32]),
+    "mhsw_run_kernel_backwards": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32, C.c_uint32, C.c_uint32]),
+    "mhsw_kernel_is_done": (C.c_int, [_P, C.POINTER(C.c_int)]),
+    "mhsw_kernel_block": (C.c_int, [_P]),
+    "mhsw_get_aln_results": (C.c_int, [_P, C.POINTER(_AlnResults)]),
+    "mhsw_align_pairs": (C.c_int, [_P, C.POINTER(PairsT), _P, C.c_int, C.c_int]),
+    "mhsw_last_timing": (C.c_int, [_P, C.POINTER(Timing)]),
+}
+
+_LIB: C.CDLL | None = None
+
+
+def load_library(path: str | Path | None = None) -> C.CDLL:
+    """Loads libmhsw.so (built in-tree by build.build()); raises if it is missing."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else _build.lib_path()
+    if not p.exists():
+        raise RuntimeError(f"libmhsw.so not found at {p}: run mhm2_staging_gb300.build.build() first")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _check(lib: C.CDLL, rc: int, handle=None, what: str = "") -> None:
+    if rc != 0:
+        msg = lib.mhsw_driver_last_error(handle).decode() if handle else ""
+        raise RuntimeError(f"{what} failed (status {rc}): {msg}")
+
+
+# ---- free functions (src/adept-sw/driver.hpp:25-35) --------------------------------
+def get_num_node_gpus() -> int:
+    lib = load_library()
+    c = C.c_int(0)
+    lib.mhsw_get_num_node_gpus(C.byref(c))
+    return c.value
+
+
+def get_tot_gpu_mem() -> int:
+    lib = load_library()
+    v = C.c_size_t(0)
+    _check(lib, lib.mhsw_get_tot_gpu_mem(C.byref(v)), what="get_tot_gpu_mem")
+    return v.value
+
+
+def get_avail_gpu_mem_per_rank(tot_ranks: int, num_devices: int = 0) -> int:
+    lib = load_library()
+    v = C.c_size_t(0)
+    _check(lib, lib.mhsw_get_avail_gpu_mem_per_rank(tot_ranks, num_devices, C.byref(v)), what="get_avail_gpu_mem")
+    return v.value
+
+
+def get_device_name(device_id: int) -> str:
+    lib = load_library()
+    buf = C.create_string_buffer(256)
+    _check(lib, lib.mhsw_get_device_name(device_id, buf, 256), what="get_device_name")
+    return buf.value.decode()
+
+
+def initialize_gpu() -> tuple[bool, float, int, int]:
+    """Returns (ok, seconds, device_count, total_mem) like initialize_gpu(double&, int&, size_t&)."""
+    lib = load_library()
+    t, c, m = C.c_double(0), C.c_int(0), C.c_size_t(0)
+    rc = lib.mhsw_initialize_gpu(C.byref(t), C.byref(c), C.byref(m))
+    return rc == 0, t.value, c.value, m.value
+
+
+def limits() -> Limits:
+    lib = load_library()
+    out = Limits()
+    lib.mhsw_limits(C.byref(out))
+    return out
+
+
+@dataclass
+class AlignmentResults:
+    """adept_sw::AlignmentResults (driver.hpp:17-23) as numpy copies, plus int32 views."""
+
+    ref_begin: np.ndarray
+    query_begin: np.ndarray
+    ref_end: np.ndarray
+    query_end: np.ndarray
+    top_scores: np.ndarray
+    ref_begin32: np.ndarray
+    query_begin32: np.ndarray
+    ref_end32: np.ndarray
+    query_end32: np.ndarray
+    top_scores32: np.ndarray
+
+
+def _as_bytes_list(seqs: Sequence[str | bytes]) -> list[bytes]:
+    return [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+
+
+class GPUDriver:
+    """Mirror of adept_sw::GPUDriver (reference src/adept-sw/driver.hpp:37-55)."""
+
+    def __init__(self) -> None:
+        self._lib = load_library()
+        h = _P()
+        _check(self._lib, self._lib.mhsw_driver_create(C.byref(h)), what="driver create")
+        self._h = h
+        self._keep: list = []
+
+    def __del__(self) -> None:
+        h = getattr(self, "_h", None)
+        if h:
+            self._lib.mhsw_driver_destroy(h)
+            self._h = None
+
+    def _ck(self, rc: int, what: str) -> None:
+        _check(self._lib, rc, self._h, what)
+
+    # GPUDriver::init (driver.cpp:198-247); returns seconds like the reference.
+    def init(self, upcxx_rank_me: int, upcxx_rank_n: int, match_score: int, mismatch_score: int,
+             gap_opening_score: int, gap_extending_score: int, rlen_limit: int) -> float:
+        t = C.c_double(0)
+        self._ck(self._lib.mhsw_driver_init(self._h, upcxx_rank_me, upcxx_rank_n, match_score, mismatch_score,
+                                            gap_opening_score, gap_extending_score, rlen_limit, C.byref(t)), "init")
+        return t.value
+
+    def set_ambiguity(self, ambiguity_score: int) -> None:
+        self._ck(self._lib.mhsw_driver_set_ambiguity(self._h, ambiguity_score), "set_ambiguity")
+
+    def set_orientation(self, orientation: int) -> None:
+        self._ck(self._lib.mhsw_driver_set_orientation(self._h, orientation), "set_orientation")
+
+    def set_form(self, form: int) -> None:
+        self._ck(self._lib.mhsw_driver_set_form(self._h, form), "set_form")
+
+    def set_int16_ceiling(self, ceiling: int) -> None:
+        self._ck(self._lib.mhsw_driver_set_int16_ceiling(self._h, ceiling), "set_int16_ceiling")
+
+    def stream(self) -> int:
+        s = _P()
+        self._ck(self._lib.mhsw_driver_stream(self._h, C.byref(s)), "stream")
+        return s.value or 0
+
+    def _marshal(self, reads: Sequence[str | bytes], contigs: Sequence[str | bytes]):
+        rb, cb = _as_bytes_list(reads), _as_bytes_list(contigs)
+        if len(rb) != len(cb):
+            raise RuntimeError("reads and contigs must have the same length")
+        n = len(cb)
+        rbufs = [C.create_string_buffer(b, len(b) + 1) for b in rb]
+        cbufs = [C.create_string_buffer(b, len(b) + 1) for b in cb]
+        rp = (C.c_char_p * max(n, 1))(*[C.cast(x, C.c_char_p) for x in rbufs])
+        cp = (C.c_char_p * max(n, 1))(*[C.cast(x, C.c_char_p) for x in cbufs])
+        rl = (C.c_int32 * max(n, 1))(*[len(b) for b in rb])
+        cl = (C.c_int32 * max(n, 1))(*[len(b) for b in cb])
+        keep = (rbufs, cbufs, rp, cp, rl, cl)
+        return n, keep
+
+    # run_kernel_forwards(reads, contigs, maxReadSize, maxContigSize) (driver.cpp:281-375)
+    def run_kernel_forwards(self, reads, contigs, max_read_size: int, max_contig_size: int) -> None:
+        n, keep = self._marshal(reads, contigs)
+        self._keep = list(keep)
+        rbufs, cbufs, rp, cp, rl, cl = keep
+        self._ck(self._lib.mhsw_run_kernel_forwards(self._h, C.cast(rp, _P), C.cast(rl, _P), C.cast(cp, _P),
+                                                    C.cast(cl, _P), n, max_read_size, max_contig_size),
+                 "run_kernel_forwards")
+
+    # run_kernel_backwards(...) (driver.cpp:377-417)
+    def run_kernel_backwards(self, reads, contigs, max_read_size: int, max_contig_size: int) -> None:
+        n, keep = self._marshal(reads, contigs)
+        rbufs, cbufs, rp, cp, rl, cl = keep
+        self._ck(self._lib.mhsw_run_kernel_backwards(self._h, C.cast(rp, _P), C.cast(rl, _P), C.cast(cp, _P),
+                                                     C.cast(cl, _P), n, max_read_size, max_contig_size),
+                 "run_kernel_backwards")
+
+    def kernel_is_done(self) -> bool:
+        d = C.c_int(0)
+        self._ck(self._lib.mhsw_kernel_is_done(self._h, C.byref(d)), "kernel_is_done")
+        return bool(d.value)
+
+    def kernel_block(self) -> None:
+        self._ck(self._lib.mhsw_kernel_block(self._h), "kernel_block")
+
+    def get_aln_results(self) -> AlignmentResults:
+        r = _AlnResults()
+        self._ck(self._lib.mhsw_get_aln_results(self._h, C.byref(r)), "get_aln_results")
+        n = r.n
+
+        def arr(ptr, dt):
+            if n == 0:
+                return np.zeros(0, dtype=dt)
+            return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dt, copy=True)
+
+        return AlignmentResults(
+            arr(r.ref_begin, np.int16), arr(r.query_begin, np.int16), arr(r.ref_end, np.int16),
+            arr(r.query_end, np.int16), arr(r.top_scores, np.int16), arr(r.ref_begin32, np.int32),
+            arr(r.query_begin32, np.int32), arr(r.ref_end32, np.int32), arr(r.query_end32, np.int32),
+            arr(r.top_scores32, np.int32))
+
+    # ---- batch entry point ---------------------------------------------------------
+    def align_pairs(self, pairs: "Pairs", form: int = FORM_PLAIN, out: np.ndarray | None = None) -> np.ndarray:
+        """Aligns host-resident pairs (A = SSW ref, B = SSW query); returns n x 5 int32
+        (score, a_begin, a_end, b_begin, b_end)."""
+        n = pairs.n
+        if out is None:
+            out = np.zeros((n, 5), dtype=np.int32)
+        pt = pairs.c_struct()
+        self._ck(self._lib.mhsw_align_pairs(self._h, C.byref(pt), out.ctypes.data_as(_P) if n else None, 1, form),
+                 "align_pairs")
+        return out
+
+    def align_pairs_device(self, dev: "DevicePairs", out_dev_ptr: int, form: int = FORM_PLAIN) -> None:
+        """Aligns pairs already resident on the device (pointers from DevicePairs);
+        results go to the device buffer out_dev_ptr (n x 5 int32)."""
+        pt = dev.c_struct()
+        self._ck(self._lib.mhsw_align_pairs(self._h, C.byref(pt), _P(out_dev_ptr), 0, form), "align_pairs (device)")
+
+    def last_timing(self) -> dict:
+        t = Timing()
+        self._ck(self._lib.mhsw_last_timing(self._h, C.byref(t)), "last_timing")
+        return t.as_dict()
+
+
+@dataclass
+class Pairs:
+    """A batch as concatenated bytes: A = SSW ref (klign: the read), B = SSW query (contig window)."""
+
+    a_seq: np.ndarray  # uint8
+    a_off: np.ndarray  # int64
+    a_len: np.ndarray  # int32
+    b_seq: np.ndarray
+    b_off: np.ndarray
+    b_len: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return int(self.a_len.shape[0])
+
+    def cells(self) -> int:
+        return int((self.a_len.astype(np.int64) * self.b_len.astype(np.int64)).sum())
+
+    def c_struct(self) -> PairsT:
+        for arr, dt in ((self.a_seq, np.uint8), (self.b_seq, np.uint8), (self.a_off, np.int64),
+                        (self.b_off, np.int64), (self.a_len, np.int32), (self.b_len, np.int32)):
+            if arr.dtype != dt or not arr.flags.c_contiguous:
+                raise RuntimeError("Pairs arrays must be contiguous with dtypes uint8/int64/int32")
+        return PairsT(self.a_seq.ctypes.data, self.a_off.ctypes.data, self.a_len.ctypes.data,
+                      self.b_seq.ctypes.data, self.b_off.ctypes.data, self.b_len.ctypes.data, self.n)
+
+    def a(self, i: int) -> bytes:
+        o = int(self.a_off[i])
+        return self.a_seq[o:o + int(self.a_len[i])].tobytes()
+
+    def b(self, i: int) -> bytes:
+        o = int(self.b_off[i])
+        return self.b_seq[o:o + int(self.b_len[i])].tobytes()
+
+    def subset(self, idx) -> "Pairs":
+        return Pairs.from_lists([self.a(int(i)) for i in idx], [self.b(int(i)) for i in idx])
+
+    @staticmethod
+    def from_lists(a: Sequence[str | bytes], b: Sequence[str | bytes]) -> "Pairs":
+        ab, bb = _as_bytes_list(a), _as_bytes_list(b)
+        if len(ab) != len(bb):
+            raise ValueError("a and b must have the same length")
+
+        def pack(xs):
+            lens = np.array([len(x) for x in xs], dtype=np.int32)
+            offs = np.zeros(len(xs), dtype=np.int64)
+            if len(xs) > 1:
+                offs[1:] = np.cumsum(lens[:-1], dtype=np.int64)
+            buf = np.frombuffer(b"".join(xs) + b"\0", dtype=np.uint8).copy()
+            return buf, offs, lens
+
+        a_seq, a_off, a_len = pack(ab)
+        b_seq, b_off, b_len = pack(bb)
+        return Pairs(a_seq, a_off, a_len, b_seq, b_off, b_len)
+
+
+@dataclass
+class DevicePairs:
+    """Device pointers of a resident batch (e.g. torch tensors' data_ptr())."""
+
+    a_seq: int
+    a_off: int
+    a_len: int
+    b_seq: int
+    b_off: int
+    b_len: int
+    n: int
+
+    def c_struct(self) -> PairsT:
+        return PairsT(self.a_seq, self.a_off, self.a_len, self.b_seq, self.b_off, self.b_len, self.n)

@@ -1,0 +1,110 @@
+"""Loader for the CPU oracles -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use this module,
+as the checker.  The product path (libmhsw.so and mhm2_staging_gb300) never imports it.
+
+  liboracle.so   C restatement of the reference SSW result contract (sw_oracle.c);
+                 pinned against the reference's own SSW and test/ssw-test.cpp's
+                 known answers (tests/golden/).
+  libssw_ref.so  the reference SSW itself (src/ssw/ssw.cpp + ssw_core.cpp), compiled
+                 from the reference checkout by oracle/Makefile; x86_64 only.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import platform
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "_build" / "liboracle.so"
+REF_SO = HERE / "_ref" / "libssw_ref.so"
+REFERENCE_ROOT = Path(os.environ.get("MHSW_REFERENCE", "/root/reference"))
+
+_P = C.c_void_p
+_ORACLE = None
+_REF = None
+
+
+def build(with_reference: bool | None = None) -> None:
+    """Builds liboracle.so, and libssw_ref.so when the reference checkout is present."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "_build/liboracle.so"], check=True)
+    if with_reference is None:
+        with_reference = (REFERENCE_ROOT / "src" / "ssw" / "ssw.cpp").exists() and platform.machine() == "x86_64"
+    if with_reference:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_ROOT}"], check=True)
+
+
+def _bind(lib: C.CDLL, name: str) -> None:
+    fn = getattr(lib, name)
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_char_p, _P, _P, C.c_char_p, _P, _P, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                   C.c_int, _P]
+
+
+def oracle_lib() -> C.CDLL:
+    global _ORACLE
+    if _ORACLE is None:
+        if not ORACLE_SO.exists():
+            build(with_reference=False)
+        lib = C.CDLL(str(ORACLE_SO))
+        _bind(lib, "sw_oracle_align_batch")
+        lib.sw_oracle_align_codes.restype = C.c_int64
+        lib.sw_oracle_align_codes.argtypes = [_P, C.c_int, _P, C.c_int, _P, C.c_int, C.c_int, _P]
+        _ORACLE = lib
+    return _ORACLE
+
+
+def reference_available() -> bool:
+    return REF_SO.exists()
+
+
+def ref_lib() -> C.CDLL:
+    global _REF
+    if _REF is None:
+        if not REF_SO.exists():
+            raise RuntimeError("reference SSW not built (oracle/_ref/libssw_ref.so)")
+        lib = C.CDLL(str(REF_SO))
+        _bind(lib, "ssw_ref_align_batch")
+        lib.ssw_ref_align.restype = C.c_int
+        lib.ssw_ref_align.argtypes = [C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.c_int, C.c_int, _P]
+        _REF = lib
+    return _REF
+
+
+def _run(lib, fn, pairs, scoring, threads):
+    n = pairs.n
+    out = np.zeros((n, 5), dtype=np.int32)
+    if n == 0:
+        return out
+    m, x, go, ge, amb = scoring
+    rc = getattr(lib, fn)(pairs.a_seq.ctypes.data_as(C.c_char_p), pairs.a_off.ctypes.data, pairs.a_len.ctypes.data,
+                          pairs.b_seq.ctypes.data_as(C.c_char_p), pairs.b_off.ctypes.data, pairs.b_len.ctypes.data,
+                          n, m, x, go, ge, amb, threads, out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"{fn} failed")
+    return out
+
+
+def align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None) -> np.ndarray:
+    """Oracle results n x 5 (score, a_begin, a_end, b_begin, b_end); scoring =
+    (match, mismatch, gap_open, gap_extend, ambiguity) as positive magnitudes."""
+    return _run(oracle_lib(), "sw_oracle_align_batch", pairs, scoring, threads or (os.cpu_count() or 1))
+
+
+def ref_align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None) -> np.ndarray:
+    """The reference SSW, called as klign calls it (src/klign.cpp:257)."""
+    return _run(ref_lib(), "ssw_ref_align_batch", pairs, scoring, threads or (os.cpu_count() or 1))
+
+
+def ref_align_one(query: bytes, ref: bytes, scoring=(1, 3, 5, 2, 2), mask_len: int = -1) -> list[int]:
+    """One reference SSW call: returns [score, ref_begin, ref_end, query_begin, query_end,
+    score2, ref_end2, mismatches]."""
+    out = (C.c_int32 * 8)()
+    m, x, go, ge, amb = scoring
+    ref_lib().ssw_ref_align(query, len(query), ref, len(ref), m, x, go, ge, amb, mask_len, C.cast(out, _P))
+    return list(out)
