@@ -1,0 +1,347 @@
+#!/usr/bin/env python
+"""Benchmark of the read-to-contig Smith-Waterman hot path on GB300.
+
+One step = one pass of the path (forward + begin pass, all pairs) over the batch of
+synthetic pairs of the uneven-length workload (4,000,000 pairs: 60% 150 bp, 30% 250 bp,
+10% 50-150 bp reads against lognormal(ln 400, 0.6) references in [64, 2048]; seed 2).
+
+  value  GCUPS of the batched form with the pairs already resident in HBM
+         (forward cells = sum len(read) * len(ref); begin-pass cells are overhead).
+  e2e    the same through the C ABI with pinned HOST buffers: copies in, both passes,
+         results out, every step.
+  plain  the plain drop-in kernel on the same pairs, for the batched-vs-plain ratio.
+
+Prints one JSON line on rank 0.  `--impl reference` times the CPU implementation of the
+path instead (the oracle port of the reference SSW, all host threads, bounded samples).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SCORING = (1, 3, 5, 2, 2)  # match, mismatch, gap open, gap extend, ambiguity (magnitudes)
+K_OPS_PER_CELL_PAIR = 6     # packed int16x2 ops per two cell updates
+WORKLOAD_NAME = "uneven read/ref lengths, 4M pairs (60% 150bp, 30% 250bp, 10% U[50,150]bp; ref lognormal(ln400,0.6) in [64,2048])"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(pairs, budget_s: float = 12.0) -> dict:
+    """The oracle port timed on the host cores on a bounded leading sample of the batch."""
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    n_probe = min(pairs.n, 2000)
+    probe = pairs.slice(0, n_probe)
+    t0 = time.perf_counter()
+    oracle.align_batch(probe, SCORING, threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    n = int(min(pairs.n, max(n_probe, n_probe * budget_s / dt)))
+    sample = pairs.slice(0, n)
+    t0 = time.perf_counter()
+    oracle.align_batch(sample, SCORING, threads)
+    dt = time.perf_counter() - t0
+    cells = sample.cells()
+    return {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
+            "sample": f"first {n} pairs of the same workload ({cells:.3g} forward cells, {dt:.1f} s)",
+            "alignments_per_s": n / dt}
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from mhm2_staging_gb300 import workloads
+    from oracle import oracle
+
+    oracle.build(with_reference=False)
+    threads = os.cpu_count() or 1
+    per_step = args.ref_pairs
+    pairs = workloads.generate(args.config, n=per_step * (args.steps + args.warmup), seed=args.config)
+    times, cells = [], []
+    for s in range(args.warmup + args.steps):
+        sub = pairs.slice(s * per_step, (s + 1) * per_step)
+        t0 = time.perf_counter()
+        oracle.align_batch(sub, SCORING, threads)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+            cells.append(sub.cells())
+    tot = sum(times)
+    gcups = sum(cells) / tot / 1e9
+    line = {
+        "impl": "reference", "metric": "GCUPS", "value": gcups, "unit": "GCUPS", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "config": {"workload": WORKLOAD_NAME, "pairs_per_step": per_step, "scoring": list(SCORING),
+                   "cache": "inputs larger than L2 (CPU run)"},
+        "alignments_per_s": per_step * args.steps / tot,
+        "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} pairs per step of the same workload (reference SSW is x86/PPC "
+                                   f"only; this is the C restatement of its result contract)"},
+        "e2e": {"value": gcups, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--pairs", type=int, default=None, help="override pairs per GPU (smaller runs)")
+    ap.add_argument("--ref-pairs", type=int, default=20000, help="pairs per step of the reference arm")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    ws, rank, local = _dist()
+    import torch
+
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from mhm2_staging_gb300 import FORM_BATCHED, FORM_PLAIN, GPUDriver, workloads
+    from mhm2_staging_gb300 import build as mbuild
+    from mhm2_staging_gb300.driver import DevicePairs, probe_dpx_rate
+
+    mbuild.build()
+    dev = torch.device("cuda", local)
+    n_per = args.pairs or workloads.CONFIG_PAIRS[args.config]
+    # weak scaling: each rank aligns its own n_per pairs (a disjoint slice of the seeded stream)
+    pairs = workloads.generate(args.config, n=n_per, first=rank * n_per)
+    cells_local = float(pairs.cells())
+
+    drv = GPUDriver()
+    drv.init(local, ws, SCORING[0], -SCORING[1], -SCORING[2], -SCORING[3], 0)
+    drv.set_ambiguity(-SCORING[4])
+    stream = torch.cuda.ExternalStream(drv.stream(), device=dev)
+
+    # resident inputs
+    tens = [torch.from_numpy(x).to(dev) for x in (pairs.a_seq, pairs.a_off, pairs.a_len, pairs.b_seq, pairs.b_off,
+                                                 pairs.b_len)]
+    out_dev = torch.empty((pairs.n, 5), dtype=torch.int32, device=dev)
+    torch.cuda.synchronize(dev)
+    dp = DevicePairs(*(t.data_ptr() for t in tens), n=pairs.n, max_a_len=int(pairs.a_len.max()),
+                     max_b_len=int(pairs.b_len.max()), cells=cells_local)
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def allmax(x: float) -> float:
+        if ws == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def allsum(x: float) -> float:
+        if ws == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        return float(t.item())
+
+    # ---- warm-up (includes the batched form's one-time launch-shape tuning) ----------
+    for _ in range(max(args.warmup, 3)):
+        drv.align_pairs_device(dp, out_dev.data_ptr(), form=FORM_BATCHED)
+
+    # ---- timed region: device-resident batched form ----------------------------------
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    fwd_ms, rev_ms, launches = [], [], 0
+    e0.record(stream)
+    for _ in range(args.steps):
+        drv.align_pairs_device(dp, out_dev.data_ptr(), form=FORM_BATCHED)
+        t = drv.last_timing()
+        fwd_ms.append(t["fwd_ms"])
+        rev_ms.append(t["rev_ms"])
+        launches += int(t["launches"])
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier()
+    clk = clocks.stop()
+    ms_local = e0.elapsed_time(e1) / args.steps
+    ms = allmax(ms_local)
+    cells_all = allsum(cells_local)
+    pairs_all = allsum(float(pairs.n))
+    gcups = cells_all / (ms * 1e-3) / 1e9
+    last = drv.last_timing()
+
+    # ---- plain drop-in kernel on the same resident pairs ------------------------------
+    plain = None
+    if not args.no_plain:
+        drv.align_pairs_device(dp, out_dev.data_ptr(), form=FORM_PLAIN)
+        torch.cuda.synchronize(dev)
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        psteps = max(1, min(args.steps, 3))
+        pf = []
+        for _ in range(psteps):
+            drv.align_pairs_device(dp, out_dev.data_ptr(), form=FORM_PLAIN)
+            pf.append(drv.last_timing()["fwd_ms"])
+        p1.record(stream)
+        torch.cuda.synchronize(dev)
+        pms = allmax(p0.elapsed_time(p1) / psteps)
+        plain = {"gcups": cells_all / (pms * 1e-3) / 1e9, "ms_per_step": pms,
+                 "fwd_kernel_gcups": cells_local / (statistics.mean(pf) * 1e-3) / 1e9}
+
+    # ---- e2e: pinned host buffers through the C ABI ------------------------------------
+    from mhm2_staging_gb300.driver import Pairs
+
+    def pinned(x: np.ndarray) -> np.ndarray:
+        t = torch.empty(x.shape, dtype={np.uint8: torch.uint8, np.int64: torch.int64,
+                                        np.int32: torch.int32}[x.dtype.type], pin_memory=True)
+        a = t.numpy()
+        a[...] = x
+        pinned.keep.append(t)
+        return a
+
+    pinned.keep = []
+    hp = Pairs(*(pinned(x) for x in (pairs.a_seq, pairs.a_off, pairs.a_len, pairs.b_seq, pairs.b_off, pairs.b_len)))
+    hout = pinned(np.zeros((pairs.n, 5), dtype=np.int32))
+    h2d = int(hp.a_seq.nbytes + hp.b_seq.nbytes + hp.a_off.nbytes + hp.b_off.nbytes + hp.a_len.nbytes +
+              hp.b_len.nbytes)
+    d2h = int(hout.nbytes)
+    drv.align_pairs(hp, form=FORM_BATCHED, out=hout)  # warm
+    barrier()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        drv.align_pairs(hp, form=FORM_BATCHED, out=hout)
+    e2e_s = allmax((time.perf_counter() - t0) / args.e2e_steps)
+    e2e_gcups = cells_all / e2e_s / 1e9
+    # the e2e results must equal the resident-input results
+    assert np.array_equal(hout, out_dev.cpu().numpy()), "e2e results differ from device-resident results"
+
+    # ---- roofline of the dominant kernel (the persistent forward kernel) -------------
+    dpx_ops, sm_hz = probe_dpx_rate(local)
+    peak_gcups = dpx_ops * 2 / K_OPS_PER_CELL_PAIR / 1e9
+    fwd_avg = statistics.mean(fwd_ms)
+    achieved = cells_local / (fwd_avg * 1e-3) / 1e9
+    alg_bytes = float(pairs.a_seq.nbytes + pairs.b_seq.nbytes + pairs.a_off.nbytes + pairs.b_off.nbytes +
+                      pairs.a_len.nbytes + pairs.b_len.nbytes + 4 * 4 * pairs.n)
+    traffic = None
+    prof = ROOT / "profiles" / "fwd_persist_traffic.json"
+    if prof.exists():
+        try:
+            pj = json.loads(prof.read_text())
+            traffic = pj["dram_bytes_per_cell"] * cells_local
+        except (KeyError, ValueError):
+            traffic = None
+    roofline = {
+        "bound": "int", "achieved": achieved, "peak": peak_gcups, "unit": "GCUPS", "frac": achieved / peak_gcups,
+        "traffic": traffic, "kernel": "k_fwd_persist (batched forward pass)",
+        "peak_basis": f"measured packed-int16 DPX add-max rate {dpx_ops / 1e12:.2f} T/s x 2 cells / "
+                      f"{K_OPS_PER_CELL_PAIR} ops per packed cell pair",
+        "hbm": {"achieved": alg_bytes / (fwd_avg * 1e-3) / 1e9, "peak": 6761.6, "unit": "GB/s",
+                "frac": alg_bytes / (fwd_avg * 1e-3) / 1e9 / 6761.6},
+    }
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(pairs)
+
+    if rank == 0:
+        line = {
+            "metric": "GCUPS", "value": gcups, "unit": "GCUPS", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int16x2 (int32 re-run on overflow)",
+            "data": "synthetic (seeded generator, workload shapes of the reference's measured configs)",
+            "config": {"workload": WORKLOAD_NAME if args.config == 2 and args.pairs is None else
+                       f"config {args.config}, {n_per} pairs per GPU", "pairs_per_gpu": n_per,
+                       "scoring": list(SCORING), "form": "batched persistent",
+                       "cache": "inputs larger than L2 (2.6 GB resident per GPU)", "parallelism": f"replicas x{ws}"},
+            "alignments_per_s": pairs_all / (ms * 1e-3),
+            "fwd_ms": statistics.mean(fwd_ms), "rev_ms": statistics.mean(rev_ms),
+            "plain": plain, "batched_vs_plain": (gcups / plain["gcups"]) if plain else None,
+            "e2e": {"value": e2e_gcups, "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_s * 1e3},
+            "gpu_launches": launches,
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "overflow16_pairs": int(last["n_overflow16"]), "rev_wavefront_pairs": int(last["n_rev_wide"]),
+            "sm_hz_probe": sm_hz,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

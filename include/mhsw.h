@@ -90,6 +90,12 @@ typedef struct {
   const int64_t *b_off;
   const int32_t *b_len;
   int64_t n;
+  /* Optional hints for device-resident batches (0 = unknown): the longest A and B
+   * and the sum of len(A)*len(B).  With both maxima given, a device batch is
+   * launched without reading its lengths back to the host. */
+  int32_t max_a_len;
+  int32_t max_b_len;
+  double cells;
 } mhsw_pairs;
 
 /* ---- free functions (src/adept-sw/driver.hpp:25-35, driver.cpp:28-77) ------- */
@@ -162,6 +168,13 @@ int mhsw_get_aln_results(mhsw_driver *drv, mhsw_aln_results *out);
  * SSW query = B; score 0 gives -1, -1, 0, 0 as SSW does). */
 int mhsw_align_pairs(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form);
 int mhsw_last_timing(mhsw_driver *drv, mhsw_timing *out);
+
+/* ---- diagnostics ----------------------------------------------------------- */
+/* Measures the device's packed int16 DPX add-max throughput (__viaddmax_s16x2 on
+ * independent chains, all SMs busy): *ops_per_s = packed instructions per second over
+ * the whole GPU, *sm_hz = SM cycles per second seen by the probe.  Basis of the
+ * cell-update roofline. */
+int mhsw_probe_dpx_rate(int device, double *ops_per_s, double *sm_hz);
 
 #ifdef __cplusplus
 }

@@ -776,6 +776,17 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
     ps.b_seq = d->b_seq.p;
     ps.b_off = d->b_off.p;
     ps.b_len = d->b_len.p;
+  } else if (pairs->max_a_len > 0 && pairs->max_b_len > 0) {
+    // device-resident inputs with size hints: no host round trip
+    ma = pairs->max_a_len;
+    mb = pairs->max_b_len;
+    cells = pairs->cells;
+    ps.a_seq = pairs->a_seq;
+    ps.a_off = pairs->a_off;
+    ps.a_len = pairs->a_len;
+    ps.b_seq = pairs->b_seq;
+    ps.b_off = pairs->b_off;
+    ps.b_len = pairs->b_len;
   } else {
     // device-resident inputs: lengths are read back once to size the launch
     std::vector<int32_t> la((size_t)n), lb((size_t)n);

@@ -75,10 +75,6 @@ struct V16 {
   __device__ static __forceinline__ T addmax_relu(T a, T b, T c) { return __viaddmax_s16x2_relu(a, b, c); }
   __device__ static __forceinline__ T addmax(T a, T b, T c) { return __viaddmax_s16x2(a, b, c); }
   __device__ static __forceinline__ T add(T a, T b) { return __viaddmax_s16x2(a, b, 0x80008000u); }
-  // Running max with "keep" predicates (keep = old >= new, i.e. no strict increase).
-  __device__ static __forceinline__ T bmax(T v, T h, bool &keep_lo, bool &keep_hi) {
-    return __vibmax_s16x2(v, h, &keep_hi, &keep_lo);
-  }
   // low half from cur, high half from prev
   __device__ static __forceinline__ T mix(T cur, T prev) { return __byte_perm(cur, prev, 0x7610); }
   // (lo: h.hi, hi: e.hi)
@@ -116,9 +112,6 @@ struct V32 {
     return T{__viaddmax_s32(a.lo, b.lo, c.lo), __viaddmax_s32(a.hi, b.hi, c.hi)};
   }
   __device__ static __forceinline__ T add(T a, T b) { return T{a.lo + b.lo, a.hi + b.hi}; }
-  __device__ static __forceinline__ T bmax(T v, T h, bool &keep_lo, bool &keep_hi) {
-    return T{__vibmax_s32(v.lo, h.lo, &keep_lo), __vibmax_s32(v.hi, h.hi, &keep_hi)};
-  }
   __device__ static __forceinline__ T mix(T cur, T prev) { return T{cur.lo, prev.hi}; }
   __device__ static __forceinline__ Pay payload(T h, T e) { return Pay{h.hi, e.hi}; }
   __device__ static __forceinline__ Pay pay_make(int h, int e) { return Pay{h, e}; }
@@ -138,7 +131,11 @@ struct V32 {
 template <class VT, int K>
 struct ProfileLayout {
   static constexpr int kWords = K * VT::kWordsPerT;                 // words per (lane, code)
-  static constexpr int kVW = (kWords % 4 == 0) ? 4 : ((kWords % 2 == 0) ? 2 : 1);
+#ifndef MHSW_PROFILE_VW_MAX
+#define MHSW_PROFILE_VW_MAX 4
+#endif
+  static constexpr int kVW = (kWords % 4 == 0 && MHSW_PROFILE_VW_MAX >= 4) ? 4
+                             : ((kWords % 2 == 0 && MHSW_PROFILE_VW_MAX >= 2) ? 2 : 1);
   static constexpr int kNQ = kWords / kVW;                          // vectors per (lane, code)
   // bytes for `lanes` lanes
   __host__ __device__ static constexpr size_t bytes(int lanes) {
@@ -162,7 +159,7 @@ struct VecW<1> {
 };
 
 template <class VT, int K>
-__device__ __forceinline__ void load_profile(const uint32_t *__restrict__ tab, int lanes, int lane_in_block, int c,
+__host__ __device__ __forceinline__ void load_profile(const uint32_t *__restrict__ tab, int lanes, int lane_in_block, int c,
                                              typename VT::T (&P)[K]) {
   using L = ProfileLayout<VT, K>;
   using Vec = typename VecW<L::kVW>::type;
@@ -186,7 +183,7 @@ __device__ __forceinline__ void load_profile(const uint32_t *__restrict__ tab, i
 }
 
 template <class VT, int K>
-__device__ __forceinline__ void store_profile_entry(uint32_t *tab, int lanes, int lane_in_block, int c, int k, int lo,
+__host__ __device__ __forceinline__ void store_profile_entry(uint32_t *tab, int lanes, int lane_in_block, int c, int k, int lo,
                                                     int hi) {
   using L = ProfileLayout<VT, K>;
   int word, nw;
@@ -210,14 +207,14 @@ __device__ __forceinline__ void store_profile_entry(uint32_t *tab, int lanes, in
 
 // Packs (value, row, col) into a key whose unsigned max is the lexicographic best:
 // larger value, then smaller row, then smaller column.  Key 0 = nothing positive.
-__device__ __forceinline__ unsigned long long best_key(int v, int row, int col) {
+__host__ __device__ __forceinline__ unsigned long long best_key(int v, int row, int col) {
   if (v <= 0) return 0ull;
   return ((unsigned long long)(unsigned)v << 40) | ((unsigned long long)(0xFFFFFu - (unsigned)row) << 20) |
          (unsigned long long)(0xFFFFFu - (unsigned)col);
 }
-__device__ __forceinline__ int key_value(unsigned long long k) { return (int)(k >> 40); }
-__device__ __forceinline__ int key_row(unsigned long long k) { return (int)(0xFFFFFu - (unsigned)((k >> 20) & 0xFFFFFu)); }
-__device__ __forceinline__ int key_col(unsigned long long k) { return (int)(0xFFFFFu - (unsigned)(k & 0xFFFFFu)); }
+__host__ __device__ __forceinline__ int key_value(unsigned long long k) { return (int)(k >> 40); }
+__host__ __device__ __forceinline__ int key_row(unsigned long long k) { return (int)(0xFFFFFu - (unsigned)((k >> 20) & 0xFFFFFu)); }
+__host__ __device__ __forceinline__ int key_col(unsigned long long k) { return (int)(0xFFFFFu - (unsigned)(k & 0xFFFFFu)); }
 
 // Sequence view with a direction: seq[i] = base[dir * i].
 struct SeqView {
@@ -343,10 +340,15 @@ __device__ void sweep_pair(const SeqView &A, const SeqView &B, const Scoring &sc
         F[k] = VT::addmax(F[k], NGE, Hg);
         Hd = H[k];
         H[k] = Hn;
-        bool keep_lo, keep_hi;
-        V[k] = VT::bmax(V[k], Hn, keep_lo, keep_hi);
-        Jlo[k] = keep_lo ? Jlo[k] : t;
-        Jhi[k] = keep_hi ? Jhi[k] : t;
+        {
+          // Strict increase of the row's running max records the step (first column).
+          // (Written as plain compares: the __vibmax_s16x2 form miscompiled once 14 or
+          // more copies were unrolled per step.)
+          const int hl = VT::lo(Hn), hh = VT::hi(Hn), vl = VT::lo(V[k]), vh = VT::hi(V[k]);
+          Jlo[k] = hl > vl ? t : Jlo[k];
+          Jhi[k] = hh > vh ? t : Jhi[k];
+          V[k] = VT::max_relu(V[k], Hn);
+        }
         Pprev[k] = Pcur[k];
       }
       Zout = VT::payload(H[K - 1], Ev);

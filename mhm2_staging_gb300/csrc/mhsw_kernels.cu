@@ -300,6 +300,7 @@ size_t group_prof_rt(bool wide32, int K) {
     case 4: return group_prof_bytes<V16, 4, kG>();
     case 5: return group_prof_bytes<V16, 5, kG>();
     case 6: return group_prof_bytes<V16, 6, kG>();
+    case 7: return group_prof_bytes<V16, 7, kG>();
     default: return group_prof_bytes<V16, 8, kG>();
   }
 }
@@ -333,6 +334,7 @@ cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfi
     else if (need <= 4) c.K = 4;
     else if (need <= 5) c.K = 5;
     else if (need <= 6) c.K = 6;
+    else if (need <= 7) c.K = 7;
     else c.K = 8;
   }
   c.pad = 2 * kG;
@@ -372,6 +374,7 @@ cudaError_t launch_forward(const FwdConfig &cfg, bool wide32, const PairSet &ps,
     case 4: return launch_fwd_t<V16, 4>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
     case 5: return launch_fwd_t<V16, 5>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
     case 6: return launch_fwd_t<V16, 6>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
+    case 7: return launch_fwd_t<V16, 7>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
     default: return launch_fwd_t<V16, 8>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
   }
 }

@@ -73,6 +73,9 @@ class PairsT(C.Structure):
         ("b_off", _P),
         ("b_len", _P),
         ("n", C.c_int64),
+        ("max_a_len", C.c_int32),
+        ("max_b_len", C.c_int32),
+        ("cells", C.c_double),
     ]
 
 
@@ -103,6 +106,7 @@ SIGNATURES: dict[str, tuple] = {
     "mhsw_get_aln_results": (C.c_int, [_P, C.POINTER(_AlnResults)]),
     "mhsw_align_pairs": (C.c_int, [_P, C.POINTER(PairsT), _P, C.c_int, C.c_int]),
     "mhsw_last_timing": (C.c_int, [_P, C.POINTER(Timing)]),
+    "mhsw_probe_dpx_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 
 _LIB: C.CDLL | None = None
@@ -167,6 +171,14 @@ def initialize_gpu() -> tuple[bool, float, int, int]:
     t, c, m = C.c_double(0), C.c_int(0), C.c_size_t(0)
     rc = lib.mhsw_initialize_gpu(C.byref(t), C.byref(c), C.byref(m))
     return rc == 0, t.value, c.value, m.value
+
+
+def probe_dpx_rate(device: int = 0) -> tuple[float, float]:
+    """(packed int16 DPX add-max instructions per second, SM cycles per second) measured on the device."""
+    lib = load_library()
+    ops, hz = C.c_double(0), C.c_double(0)
+    _check(lib, lib.mhsw_probe_dpx_rate(device, C.byref(ops), C.byref(hz)), what="probe_dpx_rate")
+    return ops.value, hz.value
 
 
 def limits() -> Limits:
@@ -343,7 +355,7 @@ class Pairs:
             if arr.dtype != dt or not arr.flags.c_contiguous:
                 raise RuntimeError("Pairs arrays must be contiguous with dtypes uint8/int64/int32")
         return PairsT(self.a_seq.ctypes.data, self.a_off.ctypes.data, self.a_len.ctypes.data,
-                      self.b_seq.ctypes.data, self.b_off.ctypes.data, self.b_len.ctypes.data, self.n)
+                      self.b_seq.ctypes.data, self.b_off.ctypes.data, self.b_len.ctypes.data, self.n, 0, 0, 0.0)
 
     def a(self, i: int) -> bytes:
         o = int(self.a_off[i])
@@ -352,6 +364,22 @@ class Pairs:
     def b(self, i: int) -> bytes:
         o = int(self.b_off[i])
         return self.b_seq[o:o + int(self.b_len[i])].tobytes()
+
+    def slice(self, lo: int, hi: int) -> "Pairs":
+        """Pairs [lo, hi) as a compact batch (offsets re-based)."""
+        hi = min(hi, self.n)
+        if hi <= lo:
+            return Pairs.from_lists([], [])
+
+        def part(seq, off, ln):
+            o, l = off[lo:hi], ln[lo:hi]
+            s0 = int(o.min())
+            s1 = int((o + l).max())
+            return np.append(seq[s0:s1], np.uint8(0)), (o - s0).astype(np.int64), l.copy()
+
+        a_seq, a_off, a_len = part(self.a_seq, self.a_off, self.a_len)
+        b_seq, b_off, b_len = part(self.b_seq, self.b_off, self.b_len)
+        return Pairs(a_seq, a_off, a_len, b_seq, b_off, b_len)
 
     def subset(self, idx) -> "Pairs":
         return Pairs.from_lists([self.a(int(i)) for i in idx], [self.b(int(i)) for i in idx])
@@ -386,6 +414,10 @@ class DevicePairs:
     b_off: int
     b_len: int
     n: int
+    max_a_len: int = 0
+    max_b_len: int = 0
+    cells: float = 0.0
 
     def c_struct(self) -> PairsT:
-        return PairsT(self.a_seq, self.a_off, self.a_len, self.b_seq, self.b_off, self.b_len, self.n)
+        return PairsT(self.a_seq, self.a_off, self.a_len, self.b_seq, self.b_off, self.b_len, self.n,
+                      self.max_a_len, self.max_b_len, self.cells)
