@@ -193,7 +193,8 @@ def main() -> None:
     out_dev = torch.empty((pairs.n, 5), dtype=torch.int32, device=dev)
     torch.cuda.synchronize(dev)
     dp = DevicePairs(*(t.data_ptr() for t in tens), n=pairs.n, max_a_len=int(pairs.a_len.max()),
-                     max_b_len=int(pairs.b_len.max()), cells=cells_local)
+                     max_b_len=int(pairs.b_len.max()), cells=cells_local,
+                     a_bytes=int((pairs.a_off + pairs.a_len).max()), b_bytes=int((pairs.b_off + pairs.b_len).max()))
 
     def barrier():
         if ws > 1:

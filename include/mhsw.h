@@ -77,7 +77,9 @@ typedef struct {
 typedef struct {
   int32_t max_b_len;       /* longest B (SSW query) the kernels accept */
   int32_t max_coord;       /* coordinates and lengths must stay below this */
-  int32_t int16_ceiling;   /* default score ceiling of the packed int16 engine */
+  int32_t int16_ceiling;   /* score ceiling of the packed int16 engine for scorings whose
+                            * mismatch and ambiguity penalties do not exceed the gap-open
+                            * penalty (the others use the unkeyed int16 engine, ceiling 16319) */
 } mhsw_limits_t;
 
 /* A batch as concatenated bytes with per-pair offsets and lengths.  Pointers are
@@ -90,12 +92,16 @@ typedef struct {
   const int64_t *b_off;
   const int32_t *b_len;
   int64_t n;
-  /* Optional hints for device-resident batches (0 = unknown): the longest A and B
-   * and the sum of len(A)*len(B).  With both maxima given, a device batch is
-   * launched without reading its lengths back to the host. */
+  /* Optional hints for device-resident batches (0 = unknown): the longest A and B,
+   * the sum of len(A)*len(B), and the byte extents of the two arenas
+   * (max over pairs of off + len).  With all four of max_a_len, max_b_len, a_bytes
+   * and b_bytes given, a device batch is launched without reading its lengths or
+   * offsets back to the host. */
   int32_t max_a_len;
   int32_t max_b_len;
   double cells;
+  int64_t a_bytes;
+  int64_t b_bytes;
 } mhsw_pairs;
 
 /* ---- free functions (src/adept-sw/driver.hpp:25-35, driver.cpp:28-77) ------- */

@@ -15,6 +15,7 @@
 
 #include "mhsw_batch.h"
 #include "mhsw_engine.cuh"
+#include "mhsw_engine16.cuh"
 #include "mhsw_launch.h"
 
 namespace mhsw {
@@ -25,7 +26,7 @@ constexpr int kGB = 16;
 constexpr int kKeyShift = 17;
 constexpr int kBucketStrip = 6;  // A longer than one K=8 strip
 constexpr int kBucketWide = 7;   // straight to int32
-constexpr int kInt16Capacity = V16::kBig - 1 - 64;
+constexpr int kInt16Capacity = kCeiling16;  // keyed int16 engine
 
 __device__ __forceinline__ int bucket_of(int M, int N, const Scoring &sc) {
   const long long bound = (long long)(M < N ? M : N) * sc.match;
@@ -67,7 +68,7 @@ __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, S
   const int grp = threadIdx.x / G;
   const int lane = threadIdx.x % G;
   const unsigned gmask = group_mask_b(G);
-  constexpr size_t kProf = group_prof_bytes<V16, 8, G>();
+  constexpr size_t kProf = group_prof16_bytes<8, G>();
   unsigned char *gbase = smem + (size_t)grp * (kProf + (size_t)bcap);
   GroupSmem gs;
   gs.prof = reinterpret_cast<uint32_t *>(gbase);
@@ -108,16 +109,16 @@ __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, S
       }
       continue;
     }
-    SeqView A{ps.a_seq + ps.a_off[p], 1, M};
-    SeqView B{ps.b_seq + ps.b_off[p], 1, N};
+    SeqView A{ps.a_code + ps.a_off[p], 1, M};
+    SeqView B{ps.b_code + ps.b_off[p], 1, N};
     SweepOut so;
     switch (bucket) {
-      case 0: sweep_pair<V16, 2, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      case 1: sweep_pair<V16, 3, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      case 2: sweep_pair<V16, 4, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      case 3: sweep_pair<V16, 5, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      case 4: sweep_pair<V16, 6, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      default: sweep_pair<V16, 8, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+      case 0: sweep16<2, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+      case 1: sweep16<3, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+      case 2: sweep16<4, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+      case 3: sweep16<5, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+      case 4: sweep16<6, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+      default: sweep16<8, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
     }
     if (lane == 0) {
       const int S = key_value(so.key);
@@ -200,7 +201,7 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     bs.err = "B longer than the kernel limit";
     return 1;
   }
-  const size_t per_group = group_prof_bytes<V16, 8, kGB>() + (size_t)bcap;
+  const size_t per_group = group_prof16_bytes<8, kGB>() + (size_t)bcap;
   auto kern = k_fwd_persist<kGB>;
 
   // keys + sort (the order is reused by every tuning trial)

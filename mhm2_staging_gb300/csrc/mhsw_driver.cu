@@ -19,6 +19,7 @@
 #include "../../include/mhsw.h"
 #include "mhsw_batch.h"
 #include "mhsw_engine.cuh"
+#include "mhsw_engine16.cuh"
 #include "mhsw_launch.h"
 
 namespace {
@@ -97,8 +98,9 @@ struct mhsw_driver {
   DBuf<int32_t> a_len, b_len;
   DBuf<int32_t> r_score, r_aend, r_bend, r_abeg, r_bbeg;
   DBuf<uint32_t> r_flag;
-  DBuf<int64_t> l_ovf, l_wide;
+  DBuf<int64_t> l_ovf, l_wide, l_esc1, l_esc2;
   DBuf<int> l_counts;
+  DBuf<uint8_t> a_code, b_code;  // base codes of the current batch
   DBuf<unsigned char> scratch;
   DBuf<unsigned char> outv;  // 5 x int16 + 5 x int32 arrays
   DBuf<int32_t> out5;
@@ -114,6 +116,7 @@ struct mhsw_driver {
   // drop-in protocol state
   int64_t n_batch = 0;
   int max_a = 0, max_b = 0;
+  int64_t a_bytes = 0, b_bytes = 0;  // arena extents of the staged batch
   bool fwd_issued = false;
   bool rev_issued = false;
   double fwd_cells = 0;
@@ -150,6 +153,10 @@ struct mhsw_driver {
     r_flag.release();
     l_ovf.release();
     l_wide.release();
+    l_esc1.release();
+    l_esc2.release();
+    a_code.release();
+    b_code.release();
     l_counts.release();
     scratch.release();
     outv.release();
@@ -198,6 +205,8 @@ int ensure_results(mhsw_driver *d, int64_t n) {
   MHSW_CK(d->r_flag.reserve((size_t)n + 1), "cudaMalloc results");
   MHSW_CK(d->l_ovf.reserve((size_t)n + 1), "cudaMalloc lists");
   MHSW_CK(d->l_wide.reserve((size_t)n + 1), "cudaMalloc lists");
+  MHSW_CK(d->l_esc1.reserve((size_t)n + 1), "cudaMalloc lists");
+  MHSW_CK(d->l_esc2.reserve((size_t)n + 1), "cudaMalloc lists");
   MHSW_CK(d->l_counts.reserve(4), "cudaMalloc lists");
   return MHSW_OK;
 }
@@ -219,6 +228,10 @@ mhsw::WorkLists work_lists(mhsw_driver *d, int64_t n) {
   wl.wide = d->l_wide.p;
   wl.ovf_count = d->l_counts.p;
   wl.wide_count = d->l_counts.p + 1;
+  wl.esc1 = d->l_esc1.p;
+  wl.esc2 = d->l_esc2.p;
+  wl.esc1_count = d->l_counts.p + 2;
+  wl.esc2_count = d->l_counts.p + 3;
   wl.cap = n;
   return wl;
 }
@@ -235,11 +248,29 @@ int ensure_scratch(mhsw_driver *d, int max_a, int max_b, mhsw::FwdConfig *c16, m
   return MHSW_OK;
 }
 
+// Translates both arenas of a batch into base codes (driver-owned buffers) and points
+// the PairSet at them.
+int translate_batch(mhsw_driver *d, mhsw::PairSet *ps, int64_t a_bytes, int64_t b_bytes) {
+  MHSW_CK(d->a_code.reserve((size_t)a_bytes + 16), "cudaMalloc codes");
+  MHSW_CK(d->b_code.reserve((size_t)b_bytes + 16), "cudaMalloc codes");
+  MHSW_CK(mhsw::launch_translate(ps->a_seq, d->a_code.p, a_bytes, d->st), "translate A");
+  MHSW_CK(mhsw::launch_translate(ps->b_seq, d->b_code.p, b_bytes, d->st), "translate B");
+  d->launches += 2;
+  ps->a_code = d->a_code.p;
+  ps->b_code = d->b_code.p;
+  return MHSW_OK;
+}
+
 // Forward pass over the staged PairSet: int16 engine, then int32 re-runs of the pairs
 // whose score crossed the ceiling.  Device-side lists; no host synchronisation.
+// Effective int16 ceiling: the keyed engine holds scores below mhsw::kCeiling16.
+int ceiling_for(mhsw_driver *d) {
+  return mhsw::keyed_scoring(d->sc) ? std::min(d->ceiling16, mhsw::kCeiling16) : d->ceiling16;
+}
+
 int run_forward(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, bool persistent_grid) {
   mhsw::FwdConfig c16, c32;
-  cudaError_t e = mhsw::plan_forward(d->device, max_a, max_b, false, &c16);
+  cudaError_t e = mhsw::plan_forward(d->device, max_a, max_b, false, &c16, mhsw::keyed_scoring(d->sc));
   if (e != cudaSuccess) return d->fail(MHSW_ERR_LIMIT, "B length %d exceeds the kernel limit %d", max_b, mhsw::kMaxB);
   e = mhsw::plan_forward(d->device, max_a, max_b, true, &c32);
   if (e != cudaSuccess) return d->fail(MHSW_ERR_LIMIT, "B length %d exceeds the kernel limit %d", max_b, mhsw::kMaxB);
@@ -254,7 +285,7 @@ int run_forward(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, b
   mhsw::ResultSet rs = result_set(d);
   mhsw::WorkLists wl = work_lists(d, ps.n);
   MHSW_CK(mhsw::reset_lists(wl, d->st), "reset lists");
-  MHSW_CK(mhsw::launch_forward(c16, false, ps, rs, d->sc, nullptr, nullptr, d->ceiling16, d->scratch.p, wl, d->st),
+  MHSW_CK(mhsw::launch_forward(c16, false, ps, rs, d->sc, nullptr, nullptr, ceiling_for(d), d->scratch.p, wl, d->st),
           "forward int16 launch");
   MHSW_CK(mhsw::launch_forward(c32, true, ps, rs, d->sc, wl.ovf, wl.ovf_count, 0x7fffffff, d->scratch.p, wl, d->st),
           "forward int32 launch");
@@ -264,11 +295,13 @@ int run_forward(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, b
 
 // Forward pass in either form; lists are reset first so both passes see fresh counters.
 int forward_any(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, int form) {
-  if (form != MHSW_FORM_BATCHED) return run_forward(d, ps, max_a, max_b, false);
+  // The batched form runs the keyed int16 engine; scorings it cannot hold (a mismatch or
+  // ambiguity penalty above the gap-open penalty) use the plain form.
+  if (form != MHSW_FORM_BATCHED || !mhsw::keyed_scoring(d->sc)) return run_forward(d, ps, max_a, max_b, false);
   mhsw::WorkLists wl = work_lists(d, ps.n);
   MHSW_CK(mhsw::reset_lists(wl, d->st), "reset lists");
   d->launches += 1;
-  if (mhsw::batched_forward(d->batch, d->device, ps, result_set(d), wl, d->sc, d->ceiling16, max_a, max_b, d->st,
+  if (mhsw::batched_forward(d->batch, d->device, ps, result_set(d), wl, d->sc, ceiling_for(d), max_a, max_b, d->st,
                             &d->launches))
     return d->fail(MHSW_ERR_CUDA, "batched forward: %s", d->batch.err.c_str());
   // int32 pass over the pairs the int16 engine could not hold
@@ -286,13 +319,13 @@ int forward_any(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, i
   return MHSW_OK;
 }
 
-int run_reverse(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b) {
+int run_reverse(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, const uint32_t *order) {
   mhsw::ResultSet rs = result_set(d);
   mhsw::WorkLists wl = work_lists(d, ps.n);
   MHSW_CK(mhsw::launch_reverse(d->device, ps, rs, d->sc, max_a, max_b, d->scratch.p,
-                               d->scratch.p ? d->scratch.cap : 0, wl, d->st),
+                               d->scratch.p ? d->scratch.cap : 0, wl, d->st, order),
           "begin pass launch");
-  d->launches += 2;
+  d->launches += 4;
   return MHSW_OK;
 }
 
@@ -378,6 +411,8 @@ int stage_strings(mhsw_driver *d, const char *const *reads, const int32_t *read_
   d->max_a = ma;
   d->max_b = mb;
   d->n_batch = n;
+  d->a_bytes = ta;
+  d->b_bytes = tb;
   double cells = 0;
   for (int32_t i = 0; i < n; i++) cells += (double)al[i] * (double)bl[i];
   d->fwd_cells = cells;
@@ -393,6 +428,8 @@ mhsw::PairSet staged_pairs(mhsw_driver *d) {
   ps.b_off = d->b_off.p;
   ps.b_len = d->b_len.p;
   ps.n = d->n_batch;
+  ps.a_code = d->a_code.p;
+  ps.b_code = d->b_code.p;
   return ps;
 }
 
@@ -481,7 +518,7 @@ int mhsw_limits(mhsw_limits_t *out) {
   if (!out) return MHSW_ERR_ARG;
   out->max_b_len = mhsw::kMaxB;
   out->max_coord = 0xFFFFF;
-  out->int16_ceiling = kInt16Ceiling;
+  out->int16_ceiling = mhsw::kCeiling16;
   return MHSW_OK;
 }
 
@@ -596,6 +633,10 @@ int mhsw_run_kernel_forwards(mhsw_driver *d, const char *const *reads, const int
   rc = stage_strings(d, reads, read_lens, contigs, contig_lens, n);
   if (rc) return rc;
   mhsw::PairSet ps = staged_pairs(d);
+  if (n > 0) {
+    rc = translate_batch(d, &ps, d->a_bytes, d->b_bytes);
+    if (rc) return rc;
+  }
   MHSW_CK(cudaEventRecord(d->ev_t[1], d->st), "event");
   if (n > 0) {
     rc = forward_any(d, ps, d->max_a, d->max_b, d->form);
@@ -643,7 +684,7 @@ int mhsw_run_kernel_backwards(mhsw_driver *d, const char *const *reads, const in
   mhsw::PairSet ps = staged_pairs(d);
   MHSW_CK(cudaEventRecord(d->ev_t[4], d->st), "event");
   if (n > 0) {
-    rc = run_reverse(d, ps, d->max_a, d->max_b);
+    rc = run_reverse(d, ps, d->max_a, d->max_b, d->form == MHSW_FORM_BATCHED ? d->batch.idx_out : nullptr);
     if (rc) return rc;
   }
   mhsw::OutViews dv, hv;
@@ -749,10 +790,10 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
   d->launches = 0;
   int ma = 0, mb = 0;
   double cells = 0;
+  int64_t ta = 0, tb = 0;
   mhsw::PairSet ps;
   MHSW_CK(cudaEventRecord(d->ev_t[0], d->st), "event");
   if (host_io) {
-    int64_t ta = 0, tb = 0;
     for (int64_t i = 0; i < n; i++) {
       const int32_t la = pairs->a_len[i], lb = pairs->b_len[i];
       if (la < 0 || lb < 0) return d->fail(MHSW_ERR_ARG, "negative length at pair %lld", (long long)i);
@@ -776,11 +817,13 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
     ps.b_seq = d->b_seq.p;
     ps.b_off = d->b_off.p;
     ps.b_len = d->b_len.p;
-  } else if (pairs->max_a_len > 0 && pairs->max_b_len > 0) {
+  } else if (pairs->max_a_len > 0 && pairs->max_b_len > 0 && pairs->a_bytes > 0 && pairs->b_bytes > 0) {
     // device-resident inputs with size hints: no host round trip
     ma = pairs->max_a_len;
     mb = pairs->max_b_len;
     cells = pairs->cells;
+    ta = pairs->a_bytes;
+    tb = pairs->b_bytes;
     ps.a_seq = pairs->a_seq;
     ps.a_off = pairs->a_off;
     ps.a_len = pairs->a_len;
@@ -788,16 +831,21 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
     ps.b_off = pairs->b_off;
     ps.b_len = pairs->b_len;
   } else {
-    // device-resident inputs: lengths are read back once to size the launch
+    // device-resident inputs: lengths and offsets are read back once to size the launch
     std::vector<int32_t> la((size_t)n), lb((size_t)n);
+    std::vector<int64_t> oa((size_t)n), ob((size_t)n);
     if (n > 0) {
       MHSW_CK(cudaMemcpyAsync(la.data(), pairs->a_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
       MHSW_CK(cudaMemcpyAsync(lb.data(), pairs->b_len, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
+      MHSW_CK(cudaMemcpyAsync(oa.data(), pairs->a_off, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
+      MHSW_CK(cudaMemcpyAsync(ob.data(), pairs->b_off, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, d->st), "D2H");
       MHSW_CK(cudaStreamSynchronize(d->st), "sync");
     }
     for (int64_t i = 0; i < n; i++) {
       ma = std::max(ma, (int)la[(size_t)i]);
       mb = std::max(mb, (int)lb[(size_t)i]);
+      ta = std::max(ta, oa[(size_t)i] + la[(size_t)i]);
+      tb = std::max(tb, ob[(size_t)i] + lb[(size_t)i]);
       cells += (double)la[(size_t)i] * (double)lb[(size_t)i];
     }
     ps.a_seq = pairs->a_seq;
@@ -811,6 +859,10 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
   if (mb > mhsw::kMaxB) return d->fail(MHSW_ERR_LIMIT, "sequence of %d bytes exceeds the limit %d", mb, mhsw::kMaxB);
   rc = ensure_results(d, n);
   if (rc) return rc;
+  if (n > 0) {
+    rc = translate_batch(d, &ps, ta, tb);
+    if (rc) return rc;
+  }
   MHSW_CK(cudaEventRecord(d->ev_t[1], d->st), "event");
   if (n > 0) {
     rc = forward_any(d, ps, ma, mb, form);
@@ -818,7 +870,7 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
   }
   MHSW_CK(cudaEventRecord(d->ev_t[2], d->st), "event");
   if (n > 0) {
-    rc = run_reverse(d, ps, ma, mb);
+    rc = run_reverse(d, ps, ma, mb, form == MHSW_FORM_BATCHED ? d->batch.idx_out : nullptr);
     if (rc) return rc;
   }
   MHSW_CK(cudaEventRecord(d->ev_t[3], d->st), "event");

@@ -216,13 +216,13 @@ __host__ __device__ __forceinline__ int key_value(unsigned long long k) { return
 __host__ __device__ __forceinline__ int key_row(unsigned long long k) { return (int)(0xFFFFFu - (unsigned)((k >> 20) & 0xFFFFFu)); }
 __host__ __device__ __forceinline__ int key_col(unsigned long long k) { return (int)(0xFFFFFu - (unsigned)(k & 0xFFFFFu)); }
 
-// Sequence view with a direction: seq[i] = base[dir * i].
+// Sequence view over base codes with a direction: seq[i] = base[dir * i].
 struct SeqView {
-  const char *base;
+  const uint8_t *base;
   int dir;  // +1 forward, -1 reversed prefix
   int len;
   __device__ __forceinline__ int code(int i) const {
-    return (i >= 0 && i < len) ? (int)c_code[(unsigned char)base[(ptrdiff_t)dir * i]] : kCodePad;
+    return (i >= 0 && i < len) ? (int)base[(ptrdiff_t)dir * i] : kCodePad;
   }
 };
 

@@ -1,0 +1,194 @@
+// mhsw_engine16.cuh -- the packed-int16 wavefront engine used for the forward pass.
+//
+// Same wavefront as sweep_pair in mhsw_engine.cuh (lane L holds rows [2KL, 2KL+2K) of a
+// strip, low halves at column j, high halves at column j-1, lane L two steps behind
+// lane L-1), with three changes that take work off the integer ALU pipe:
+//
+//  1. Gap values are kept biased by the gap-open penalty: X^ = X + gO for X in {E, F}.
+//     Then X^' = max(X^ - gE, H) uses H directly, and
+//       H = max(max(Hdiag + s + gO, E^, F^) - gO, 0)
+//     is one 3-way max and one add-max-relu.  Hdiag + s + gO is formed with integer
+//     multiply-adds (FMA pipe) from two table words, one per half, each already
+//     biased by +gO; this needs s + gO >= 0 for every score (mismatch and ambiguity
+//     not above the gap-open penalty), which the driver checks before choosing this
+//     engine.  PAD cells score -gO (biased 0), which keeps every value outside the
+//     matrix below the pair's maximum.
+//  2. The arg-max is tracked per lane half, not per row: each cell contributes the
+//     16-bit key H*8 + (7-k) (k = row within the half), so the maximum key is the
+//     largest score at the smallest row; the half's running key is kept with the step
+//     at which it last strictly grew.  Because steps are columns, that step is the
+//     first column at which that row reached that score -- the lexicographic rule of
+//     SSW (ssw_core.cpp:474-506).  Keys need H < 4096, so this engine flags pairs whose
+//     score reaches the ceiling (at most kCeiling16) for the int32 engine.
+//  3. The profile table holds separate low-half and high-half words, loaded as 128-bit
+//     vectors; the high words loaded at step t serve the high half at step t+1.
+#pragma once
+#include "mhsw_engine.cuh"
+
+namespace mhsw {
+
+constexpr int kCeiling16 = 4000;  // largest score the keyed int16 engine accepts
+
+template <int K>
+struct Prof16 {
+  static constexpr int kWords = ((2 * K + 3) / 4) * 4;  // lo words [0,K), hi words [K,2K), padded
+  static constexpr int kNQ = kWords / 4;
+  __host__ __device__ static constexpr size_t bytes(int lanes) { return (size_t)kNumCodes * kNQ * lanes * 16; }
+};
+
+template <int KMAX, int G>
+__host__ __device__ constexpr size_t group_prof16_bytes() {
+  return Prof16<KMAX>::bytes(G);
+}
+
+__device__ __forceinline__ uint32_t sign_mask16(uint32_t x) {
+  // each 16-bit half -> 0xffff if its bit 15 is set, else 0 (PRMT sign-replicate mode)
+  uint32_t r;
+  asm("prmt.b32 %0, %1, %2, 0xBB99;" : "=r"(r) : "r"(x), "r"(0u));
+  return r;
+}
+
+template <int K, int G>
+__device__ void sweep16(const SeqView &A, const SeqView &B, const Scoring &sc, const GroupSmem &gs, int lane,
+                        unsigned gmask, V16::Pay *bnd, int ceiling, SweepOut &out) {
+  using L = Prof16<K>;
+  constexpr int RS = 2 * K * G;
+  const int M = A.len, N = B.len;
+  const uint32_t NGE = V16::splat(-sc.gap_extend);
+  const uint32_t NGO = V16::splat(-sc.gap_open);
+
+  // B codes into shared memory: bcodes[pad + j] for j in [-pad, N + 2G); PAD outside [0, N).
+  const int fill = gs.pad + N + 2 * G < gs.bcap ? gs.pad + N + 2 * G : gs.bcap;
+  for (int x = lane; x < fill; x += G) gs.bcodes[x] = (uint8_t)B.code(x - gs.pad);
+  __syncwarp(gmask);
+
+  unsigned long long best = 0ull;
+  int overflow = 0;
+  const int nstrips = (M + RS - 1) / RS;
+  const int T_end = N + 2 * G - 1;
+  const uint4 *tab = reinterpret_cast<const uint4 *>(gs.prof);
+  const uint8_t *bc = gs.bcodes + gs.pad - 2 * lane;  // bc[t] = code of this lane's lo column at step t
+
+  for (int s = 0; s < nstrips; s++) {
+    const int row0 = s * RS + lane * 2 * K;
+    __syncwarp(gmask);
+    // Profile words: lo word k = s(A[row0+k], c) + gO; hi word k = (s(A[row0+K+k], c) + gO) << 16.
+    {
+      uint32_t *tw = gs.prof;
+      for (int c = 0; c < kNumCodes; c++) {
+#pragma unroll
+        for (int w = 0; w < L::kWords; w++) {
+          uint32_t v = 0;
+          if (w < K) {
+            v = (uint32_t)(sub_score(A.code(row0 + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu;
+          } else if (w < 2 * K) {
+            v = ((uint32_t)(sub_score(A.code(row0 + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu) << 16;
+          }
+          const int q = w / 4, r = w % 4;
+          tw[((c * L::kNQ + q) * G + lane) * 4 + r] = v;
+        }
+      }
+    }
+    __syncwarp(gmask);
+
+    uint32_t H[K], F[K], Phi[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      H[k] = 0u;
+      F[k] = 0u;    // F^ = F + gO with F = -gO before column 0
+      Phi[k] = 0u;  // hi words of the PAD column before column 0 (score -gO, biased 0)
+    }
+    uint32_t Hlast = 0u, Ecout = 0u, HtopPrev = 0u;
+    uint32_t Zout = 0u;  // (lo: H of the hi-last row, hi: E^ below it)
+    uint32_t Kl = 0u;    // running key per half
+    uint32_t Jp = 0u;    // step of the last strict increase of Kl, per half
+    const bool first_strip = (s == 0);
+    const bool last_strip = (s == nstrips - 1);
+
+    for (int t = 0; t < T_end; t++) {
+      const int c = bc[t];
+      uint32_t w[L::kWords];
+#pragma unroll
+      for (int q = 0; q < L::kNQ; q++) {
+        const uint4 v = tab[(c * L::kNQ + q) * G + lane];
+        w[4 * q + 0] = v.x;
+        w[4 * q + 1] = v.y;
+        w[4 * q + 2] = v.z;
+        w[4 * q + 3] = v.w;
+      }
+      uint32_t z = __shfl_up_sync(gmask, Zout, 1, G);
+      if (lane == 0) {
+        z = 0u;
+        if (!first_strip) {
+          const int j = t;
+          if (j < N) z = bnd[j];
+        }
+      }
+      uint32_t Ev = __byte_perm(z, Ecout, 0x5432);        // lo: from the left lane, hi: own lo half
+      const uint32_t Htop = __byte_perm(z, Hlast, 0x5410);
+      uint32_t Hd = HtopPrev;
+      HtopPrev = Htop;
+      uint32_t key[K];
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        const uint32_t Q = Hd + w[k] + Phi[k];  // halves never carry: all terms >= 0, sum < 2^15
+        const uint32_t m = __vimax3_s16x2(Q, Ev, F[k]);
+        const uint32_t Hn = __viaddmax_s16x2_relu(m, NGO, 0u);
+        Ev = __viaddmax_s16x2(Ev, NGE, Hn);
+        F[k] = __viaddmax_s16x2(F[k], NGE, Hn);
+        Hd = H[k];
+        H[k] = Hn;
+        key[k] = Hn * 8u + (uint32_t)(7 - k) * 0x00010001u;
+        Phi[k] = w[K + k];
+      }
+      uint32_t km = key[0];
+#pragma unroll
+      for (int k = 1; k + 1 < K; k += 2) km = __vimax3_s16x2(km, key[k], key[k + 1]);
+      if ((K % 2) == 0) km = __vimax_s16x2_relu(km, key[K - 1]);
+      Zout = __byte_perm(H[K - 1], Ev, 0x7632);
+      Hlast = H[K - 1];
+      Ecout = Ev;
+      // running key per half; record the step where it strictly grows
+      const uint32_t Kn = __vimax_s16x2_relu(Kl, km);
+      const uint32_t msk = sign_mask16(Kn - Kl + 0x7fff7fffu);
+      const uint32_t tt = (uint32_t)t * 0x00010001u;
+      Jp = (msk & tt) | (~msk & Jp);
+      Kl = Kn;
+      if (!last_strip && lane == G - 1) {
+        const int jh = t - 2 * lane - 1;  // hi-half column of the last lane
+        if (jh >= 0 && jh < N) bnd[jh] = Zout;
+      }
+    }
+
+    // Decode the two halves' keys into (value, row, column) and reduce over the group.
+    unsigned long long kbest = 0ull;
+    int vmax_lane = 0;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+      const uint32_t key = half ? (Kl >> 16) : (Kl & 0xffffu);
+      const int v = (int)(key >> 3);
+      const int k = 7 - (int)(key & 7u);
+      const int r = row0 + (half ? K : 0) + k;
+      const int jstep = (int)(half ? (Jp >> 16) : (Jp & 0xffffu));
+      const int col = jstep - 2 * lane - half;
+      if (v > vmax_lane) vmax_lane = v;  // every key counts for the overflow test (PAD rows included)
+      if (v > 0 && r < M) {
+        const unsigned long long kk = best_key(v, r, col);
+        if (kk > kbest) kbest = kk;
+      }
+    }
+    if (vmax_lane > ceiling) overflow = 1;
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+      const unsigned long long other = __shfl_xor_sync(gmask, kbest, o, G);
+      kbest = other > kbest ? other : kbest;
+      overflow |= __shfl_xor_sync(gmask, overflow, o, G);
+    }
+    if (kbest > best) best = kbest;
+    __syncwarp(gmask);
+  }
+  out.key = best;
+  out.overflow = overflow;
+}
+
+}  // namespace mhsw

@@ -7,15 +7,17 @@
 //            prefixes A[0..a_end], B[0..b_end] (the reference's reverse pass,
 //            src/ssw/ssw_core.cpp:1166-1178 and src/adept-sw/kernel.cpp:335-509).
 //            Exact: every cell holding the score lies on an alignment from the end
-//            cell whose total gap length g obeys g*min(gO,gE) <= (a_end+1)*match - score,
+//            cell whose total gap length g obeys g*min(gO,gE) <= D*match - score with
+//            D <= min(a_end+1, b_end+1) diagonal steps,
 //            so the band |j - i| <= g contains it and banding only lowers other cells.
 //            k_rev_wave runs the wavefront engine on the reversed box for the rare
-//            pairs whose band is wider than kBandMax.
+//            pairs whose band is wider than the widest banded instantiation.
 // Output   : k_finalize / k_pack5  -- orientation mapping into the caller's arrays.
 #include <algorithm>
 #include <cstdio>
 
 #include "mhsw_engine.cuh"
+#include "mhsw_engine16.cuh"
 #include "mhsw_launch.h"
 
 namespace mhsw {
@@ -75,8 +77,8 @@ __global__ void __launch_bounds__(256) k_fwd(PairSet ps, ResultSet rs, Scoring s
       }
       continue;
     }
-    SeqView A{ps.a_seq + ps.a_off[p], 1, M};
-    SeqView B{ps.b_seq + ps.b_off[p], 1, N};
+    SeqView A{ps.a_code + ps.a_off[p], 1, M};
+    SeqView B{ps.b_code + ps.b_off[p], 1, N};
     SweepOut so;
     sweep_pair<VT, K, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so);
     if (lane == 0) {
@@ -98,84 +100,227 @@ __global__ void __launch_bounds__(256) k_fwd(PairSet ps, ResultSet rs, Scoring s
   }
 }
 
-// One thread per pair: banded begin search (see file header).
-__global__ void __launch_bounds__(128) k_rev_banded(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl) {
-  constexpr int NEG = -(1 << 29);
-  const int gO = sc.gap_open, gE = sc.gap_extend;
-  const int gmin = gO < gE ? gO : gE;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < ps.n; p += (int64_t)gridDim.x * blockDim.x) {
-    const int S = rs.score[p];
-    if (rs.flag[p] & kFlagTooLong) {
-      rs.a_beg[p] = -1;
-      rs.b_beg[p] = 0;
+// Plain forward pass with the keyed int16 engine (mhsw_engine16.cuh): one G-lane group
+// per pair, grid-stride over [0, n).
+template <int K, int G>
+__global__ void __launch_bounds__(256) k_fwd16(PairSet ps, ResultSet rs, Scoring sc, int ceiling, V16::Pay *scratch,
+                                               int scratch_stride, WorkLists wl, int pad, int bcap) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int gpb = blockDim.x / G;
+  const int grp = threadIdx.x / G;
+  const int lane = threadIdx.x % G;
+  const unsigned gmask = group_mask(G);
+  constexpr size_t kProf = group_prof16_bytes<K, G>();
+  unsigned char *gbase = smem + (size_t)grp * (kProf + (size_t)bcap);
+  GroupSmem gs;
+  gs.prof = reinterpret_cast<uint32_t *>(gbase);
+  gs.prof_lanes = G;
+  gs.bcodes = gbase + kProf;
+  gs.pad = pad;
+  gs.bcap = bcap;
+  constexpr int RS = 2 * K * G;
+  const int64_t gid = (int64_t)blockIdx.x * gpb + grp;
+  const int64_t gstride = (int64_t)gridDim.x * gpb;
+  V16::Pay *bnd = scratch ? scratch + gid * (int64_t)scratch_stride : nullptr;
+  for (int64_t p = gid; p < ps.n; p += gstride) {
+    const int M = ps.a_len[p], N = ps.b_len[p];
+    const bool too_long = (N > bcap - pad - 2 * G) || (M > RS && (bnd == nullptr || N > scratch_stride));
+    if (M <= 0 || N <= 0 || too_long) {
+      if (lane == 0) {
+        rs.score[p] = 0;
+        rs.a_end[p] = -1;
+        rs.b_end[p] = 0;
+        rs.flag[p] = too_long ? kFlagTooLong : 0u;
+      }
       continue;
     }
-    if (S <= 0) {
+    SeqView A{ps.a_code + ps.a_off[p], 1, M};
+    SeqView B{ps.b_code + ps.b_off[p], 1, N};
+    SweepOut so;
+    sweep16<K, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so);
+    if (lane == 0) {
+      const int S = key_value(so.key);
+      if (so.overflow) {
+        rs.flag[p] = kFlagOverflow16;
+        const int slot = atomicAdd(wl.ovf_count, 1);
+        if (slot < wl.cap) wl.ovf[slot] = p;
+        rs.score[p] = S;
+        rs.a_end[p] = -1;
+        rs.b_end[p] = 0;
+      } else {
+        rs.flag[p] = 0u;
+        rs.score[p] = S;
+        rs.a_end[p] = S > 0 ? key_row(so.key) : -1;
+        rs.b_end[p] = S > 0 ? key_col(so.key) : 0;
+      }
+    }
+  }
+}
+
+// One thread per pair: banded begin search (see file header).  The band is WB-1 cells
+// wide (half-width G = WB/2 - 1) and lives in registers, fully unrolled; the codes of a
+// row's band are loaded before its dependency chain starts.  Rows whose band lies
+// inside [0, N2) run without bound checks.  The row cap t starts at 2*score/match + 16
+// and doubles until a row reaches the score, so short low-score alignments stay in a
+// narrow band.  Pairs that need a band wider than this instantiation holds go to
+// out_list for the next wider one.
+template <int WB>
+__device__ __forceinline__ void band_row(const uint8_t *__restrict__ b, int i, int N2, uint32_t rp0, uint32_t rp1,
+                                         int gO, int gE, int (&H)[WB], int (&E)[WB], int &rowmax, bool edge) {
+  constexpr int NEG = -(1 << 28);
+  constexpr int G = WB / 2 - 1;
+  constexpr int W = 2 * G + 1;
+  const int jlo = i - G;
+  int cb[W];
+#pragma unroll
+  for (int d = 0; d < W; d++) {
+    int j = jlo + d;
+    if (edge) j = j < 0 ? 0 : (j >= N2 ? N2 - 1 : j);
+    cb[d] = b[-j];
+  }
+  int F = NEG;
+  int rm = 0;
+#pragma unroll
+  for (int d = 0; d < W; d++) {
+    const int s = (int)__byte_perm(rp0, rp1, 0x7770u | (uint32_t)cb[d]) - 128;
+    const int e = __viaddmax_s32(E[d + 1], -gE, H[d + 1] - gO);
+    int h = __vimax3_s32_relu(H[d] + s, e, F);
+    int f = __viaddmax_s32(F, -gE, h - gO);
+    if (edge) {
+      const int j = jlo + d;
+      const bool left = j < 0;
+      h = left ? 0 : h;
+      E[d] = left ? NEG : e;
+      F = left ? -gO : f;
+      rm = (j < N2) ? max(rm, h) : rm;
+    } else {
+      E[d] = e;
+      F = f;
+      rm = max(rm, h);
+    }
+    H[d] = h;
+  }
+  rowmax = rm;
+}
+
+template <int WB>
+__global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scoring sc,
+                                                  const uint32_t *__restrict__ order,
+                                                  const int64_t *__restrict__ in_list, const int *__restrict__ in_count,
+                                                  int64_t *out_list, int *out_count, int64_t cap) {
+  constexpr int NEG = -(1 << 28);
+  constexpr int G = WB / 2 - 1;
+  constexpr int W = 2 * G + 1;
+  const int gO = sc.gap_open, gE = sc.gap_extend, mt = sc.match;
+  const int gmin = gO < gE ? gO : gE;
+  int64_t total = ps.n;
+  if (in_list) {
+    total = *in_count;
+    if (total > cap) total = cap;
+  }
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = in_list ? in_list[idx] : (order ? (int64_t)order[idx] : idx);
+    const int S = rs.score[p];
+    if (!in_list && ((rs.flag[p] & kFlagTooLong) || S <= 0)) {
       rs.a_beg[p] = -1;
       rs.b_beg[p] = 0;
       continue;
     }
     const int ie = rs.a_end[p], je = rs.b_end[p];
     const int M2 = ie + 1, N2 = je + 1;
-    long long gbl = ((long long)M2 * sc.match - S) / (gmin > 0 ? gmin : 1);
-    if (gbl < 0) gbl = 0;
-    if (gbl > (long long)M2 + N2) gbl = (long long)M2 + N2;
-    const int gb = (int)gbl;
-    const int W = 2 * gb + 1;
-    if (W > kBandMax) {
-      rs.flag[p] |= kFlagRevWide;
-      const int slot = atomicAdd(wl.wide_count, 1);
-      if (slot < wl.cap) wl.wide[slot] = p;
-      continue;
-    }
-    int Harr[kBandMax + 1], Earr[kBandMax + 1];
-    for (int d = 0; d <= W; d++) {
-      Harr[d] = 0;
-      Earr[d] = NEG;
-    }
-    const char *a = ps.a_seq + ps.a_off[p];
-    const char *b = ps.b_seq + ps.b_off[p];
-    int best = 0, bi = -1, bj = 0;
-    for (int i = 0; i < M2; i++) {
-      const int ca = c_code[(unsigned char)a[ie - i]];
-      const int jlo = i - gb;
-      int F = NEG;
-      for (int d = 0; d < W; d++) {
-        const int j = jlo + d;
-        if (j >= N2) break;
-        if (j < 0) {
-          Harr[d] = 0;
-          Earr[d] = NEG;
-          F = -gO;
-          continue;
+    const uint8_t *a = ps.a_code + ps.a_off[p] + ie;  // reversed: a[-i]
+    const uint8_t *b = ps.b_code + ps.b_off[p] + je;  // reversed: b[-j]
+    long long tt = 2ll * S / (mt > 0 ? mt : 1) + 16;
+    int t = (int)(tt < M2 ? tt : M2);
+    int fi = -1, fj = -1;
+    bool escalate = false, found = false;
+    for (;;) {
+      // diagonal steps D <= min(rows, columns) of the box; gaps total <= (D*match - S)/gmin
+      const long long dmax = t < N2 ? t : N2;
+      long long g = (dmax * mt - S) / (gmin > 0 ? gmin : 1);
+      if (g > G) {
+        escalate = true;
+        break;
+      }
+      int H[W + 1], E[W + 1];
+#pragma unroll
+      for (int d = 0; d <= W; d++) {
+        H[d] = 0;
+        E[d] = NEG;
+      }
+      for (int i = 0; i < t; i++) {
+        const int ca = a[-i];
+        uint32_t rp0 = 0, rp1 = 0;  // s(ca, cb) + 128 as bytes 0..4 of {rp0, rp1}
+#pragma unroll
+        for (int c = 0; c < 5; c++) {
+          const uint32_t v = (uint32_t)(sub_score(ca, c, sc, 1 << 20) + 128) & 0xffu;
+          if (c < 4) rp0 |= v << (8 * c);
+          else rp1 = v;
         }
-        const int hdiag = Harr[d], hup = Harr[d + 1], eup = Earr[d + 1];
-        const int cb = c_code[(unsigned char)b[je - j]];
-        const int e = max(eup - gE, hup - gO);
-        int h = hdiag + sub_score(ca, cb, sc, 1 << 28);
-        h = max(h, e);
-        h = max(h, F);
-        h = max(h, 0);
-        Harr[d] = h;
-        Earr[d] = e;
-        F = max(F - gE, h - gO);
-        if (h > best) {
-          best = h;
-          bi = i;
-          bj = j;
+        int rowmax;
+        const bool edge = (i - G < 0) || (i + G >= N2);
+        if (edge) band_row<W + 1>(b, i, N2, rp0, rp1, gO, gE, H, E, rowmax, true);
+        else band_row<W + 1>(b, i, N2, rp0, rp1, gO, gE, H, E, rowmax, false);
+        if (rowmax >= S) {
+          // first cell of this row that reaches the score
+#pragma unroll
+          for (int d = 0; d < W; d++) {
+            const int j = i - G + d;
+            if (!found && j >= 0 && j < N2 && H[d] >= S) {
+              found = true;
+              fi = i;
+              fj = j;
+            }
+          }
+          break;
         }
       }
-      if (best >= S) break;
+      if (found || t >= M2) break;
+      t = (2 * t < M2) ? 2 * t : M2;
     }
-    if (best != S) {
+    if (escalate) {
+      const int slot = atomicAdd(out_count, 1);
+      if (slot < cap) out_list[slot] = p;
+      continue;
+    }
+    if (!found) {
       rs.flag[p] |= kFlagTooLong;  // inconsistent; reported as an error by the driver
       rs.a_beg[p] = -1;
       rs.b_beg[p] = 0;
       continue;
     }
-    rs.a_beg[p] = ie - bi;
-    rs.b_beg[p] = je - bj;
+    rs.a_beg[p] = ie - fi;
+    rs.b_beg[p] = je - fj;
   }
+}
+
+// Byte arena -> SSW base codes (0..4), 16 bytes per thread step when aligned.
+__global__ void k_translate(const char *__restrict__ src, uint8_t *__restrict__ dst, int64_t nbytes, int vec) {
+  __shared__ uint8_t tab[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) tab[i] = c_code[i];
+  __syncthreads();
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t done = 0;
+  if (vec) {
+    const int64_t n16 = nbytes / 16;
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+    for (int64_t i = tid; i < n16; i += stride) {
+      uint4 v = s4[i];
+      uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const uint32_t x = w[q];
+        w[q] = (uint32_t)tab[x & 0xff] | ((uint32_t)tab[(x >> 8) & 0xff] << 8) | ((uint32_t)tab[(x >> 16) & 0xff] << 16) |
+               ((uint32_t)tab[x >> 24] << 24);
+      }
+      d4[i] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    done = n16 * 16;
+  }
+  for (int64_t i = done + tid; i < nbytes; i += stride) dst[i] = tab[(unsigned char)src[i]];
 }
 
 // Wavefront begin search on the reversed box for the pairs listed in wl.wide.
@@ -207,7 +352,8 @@ __global__ void __launch_bounds__(256) k_rev_wave(PairSet ps, ResultSet rs, Scor
     const int S = rs.score[p];
     const int ie = rs.a_end[p], je = rs.b_end[p];
     const int M2 = ie + 1;
-    long long gbl = ((long long)M2 * sc.match - S) / (gmin > 0 ? gmin : 1);
+    const long long dmax = M2 < je + 1 ? M2 : je + 1;
+    long long gbl = (dmax * sc.match - S) / (gmin > 0 ? gmin : 1);
     if (gbl < 0) gbl = 0;
     long long n2 = (long long)M2 + gbl + 1;
     if (n2 > je + 1) n2 = je + 1;
@@ -221,8 +367,8 @@ __global__ void __launch_bounds__(256) k_rev_wave(PairSet ps, ResultSet rs, Scor
       }
       continue;
     }
-    SeqView A{ps.a_seq + ps.a_off[p] + ie, -1, M2};
-    SeqView B{ps.b_seq + ps.b_off[p] + je, -1, N2};
+    SeqView A{ps.a_code + ps.a_off[p] + ie, -1, M2};
+    SeqView B{ps.b_code + ps.b_off[p] + je, -1, N2};
     SweepOut so;
     sweep_pair<V32, K, G>(A, B, sc, gs, lane, gmask, bnd, 0x7fffffff, so);
     if (lane == 0) {
@@ -279,6 +425,8 @@ __global__ void k_pack5(ResultSet rs, int64_t n, int32_t *out5) {
 __global__ void k_reset_lists(WorkLists wl) {
   *wl.ovf_count = 0;
   *wl.wide_count = 0;
+  *wl.esc1_count = 0;
+  *wl.esc2_count = 0;
 }
 
 int g_num_sms = 0;
@@ -290,6 +438,18 @@ int num_sms(int device) {
     g_num_sms = v > 0 ? v : 1;
   }
   return g_num_sms;
+}
+
+size_t group_prof16_rt(int K) {
+  switch (K) {
+    case 2: return group_prof16_bytes<2, kG>();
+    case 3: return group_prof16_bytes<3, kG>();
+    case 4: return group_prof16_bytes<4, kG>();
+    case 5: return group_prof16_bytes<5, kG>();
+    case 6: return group_prof16_bytes<6, kG>();
+    case 7: return group_prof16_bytes<7, kG>();
+    default: return group_prof16_bytes<8, kG>();
+  }
 }
 
 size_t group_prof_rt(bool wide32, int K) {
@@ -320,9 +480,27 @@ cudaError_t launch_fwd_t(const FwdConfig &cfg, const PairSet &ps, const ResultSe
   return cudaGetLastError();
 }
 
+template <int K>
+cudaError_t launch_fwd16_t(const FwdConfig &cfg, const PairSet &ps, const ResultSet &rs, const Scoring &sc,
+                           int ceiling, void *scratch, int scratch_stride, const WorkLists &wl, cudaStream_t st) {
+  auto kern = k_fwd16<K, kG>;
+  if (cfg.smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+    if (e != cudaSuccess) return e;
+  }
+  kern<<<cfg.grid, cfg.groups_per_block * kG, cfg.smem, st>>>(ps, rs, sc, ceiling,
+                                                              reinterpret_cast<V16::Pay *>(scratch), scratch_stride,
+                                                              wl, cfg.pad, cfg.bcap);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
-cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg) {
+bool keyed_scoring(const Scoring &sc) {
+  return sc.mismatch <= sc.gap_open && sc.ambiguity <= sc.gap_open && sc.gap_open >= 1 && sc.gap_extend >= 1;
+}
+
+cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg, bool keyed) {
   FwdConfig c{};
   c.G = kG;
   if (wide32) {
@@ -342,7 +520,7 @@ cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfi
   if (max_b > kMaxB) return cudaErrorInvalidValue;
   c.bcap = ((c.pad + max_b + 2 * kG) + 15) / 16 * 16;
   const size_t budget = 100 * 1024;  // keep two blocks per SM possible
-  const size_t per_group = group_prof_rt(wide32, c.K) + (size_t)c.bcap;
+  const size_t per_group = ((keyed && !wide32) ? group_prof16_rt(c.K) : group_prof_rt(wide32, c.K)) + (size_t)c.bcap;
   int gpb = 8;
   while (gpb > 1 && (size_t)gpb * per_group > budget) gpb /= 2;
   c.groups_per_block = gpb;
@@ -350,6 +528,7 @@ cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfi
   if (c.smem > 220 * 1024) return cudaErrorInvalidValue;
   int sms = num_sms(device);
   c.grid = sms * 8;  // grid-stride; callers may lower it
+  c.keyed = keyed && !wide32;
   *cfg = c;
   return cudaSuccess;
 }
@@ -368,6 +547,17 @@ cudaError_t launch_forward(const FwdConfig &cfg, bool wide32, const PairSet &ps,
   // scratch stride (payloads per group) = B capacity
   const int stride = cfg.bcap;
   if (wide32) return launch_fwd_t<V32, 4>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
+  if (cfg.keyed && !list) {
+    switch (cfg.K) {
+      case 2: return launch_fwd16_t<2>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+      case 3: return launch_fwd16_t<3>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+      case 4: return launch_fwd16_t<4>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+      case 5: return launch_fwd16_t<5>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+      case 6: return launch_fwd16_t<6>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+      case 7: return launch_fwd16_t<7>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+      default: return launch_fwd16_t<8>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+    }
+  }
   switch (cfg.K) {
     case 2: return launch_fwd_t<V16, 2>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
     case 3: return launch_fwd_t<V16, 3>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
@@ -380,12 +570,18 @@ cudaError_t launch_forward(const FwdConfig &cfg, bool wide32, const PairSet &ps,
 }
 
 cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, const Scoring &sc, int max_a,
-                           int max_b, void *scratch, size_t scratch_bytes, const WorkLists &wl, cudaStream_t st) {
+                           int max_b, void *scratch, size_t scratch_bytes, const WorkLists &wl, cudaStream_t st,
+                           const uint32_t *order) {
+  const int sms = num_sms(device);
   if (ps.n > 0) {
-    int sms = num_sms(device);
-    int64_t blocks = (ps.n + 127) / 128;
-    int grid = (int)std::min<int64_t>(blocks, (int64_t)sms * 16);
-    k_rev_banded<<<grid, 128, 0, st>>>(ps, rs, sc, wl);
+    const int64_t blocks = (ps.n + 127) / 128;
+    const int grid = (int)std::min<int64_t>(blocks, (int64_t)sms * 16);
+    const int gridl = sms * 8;
+    k_rev_band<16><<<grid, 128, 0, st>>>(ps, rs, sc, order, nullptr, nullptr, wl.esc1, wl.esc1_count, wl.cap);
+    k_rev_band<32><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, wl.esc1, wl.esc1_count, wl.esc2, wl.esc2_count,
+                                          wl.cap);
+    k_rev_band<64><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, wl.esc2, wl.esc2_count, wl.wide, wl.wide_count,
+                                          wl.cap);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -397,7 +593,6 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
   int stride = c.bcap;
   V32::Pay *scr = nullptr;
   if (max_a > RS) {
-    // reuse the caller's scratch if it is large enough for a reduced grid
     size_t per_group = (size_t)stride * sizeof(V32::Pay);
     int groups = scratch ? (int)std::min<size_t>(scratch_bytes / per_group, (size_t)c.grid * c.groups_per_block) : 0;
     if (groups >= c.groups_per_block) {
@@ -405,13 +600,22 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
       scr = reinterpret_cast<V32::Pay *>(scratch);
     }
   }
-  c.grid = std::max(1, std::min(c.grid, num_sms(device) * 4));
+  c.grid = std::max(1, std::min(c.grid, sms * 4));
   auto kern = k_rev_wave<4, kG>;
   if (c.smem > 48 * 1024) {
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
     if (e != cudaSuccess) return e;
   }
   kern<<<c.grid, c.groups_per_block * kG, c.smem, st>>>(ps, rs, sc, wl, scr, stride, c.pad, c.bcap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_translate(const char *src, uint8_t *dst, int64_t nbytes, cudaStream_t st) {
+  if (nbytes <= 0) return cudaSuccess;
+  const int vec = ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) % 16 == 0) ? 1 : 0;
+  const int64_t work = vec ? (nbytes / 16 + 1) : nbytes;
+  const int grid = (int)std::min<int64_t>((work + 255) / 256, 152 * 16);
+  k_translate<<<grid, 256, 0, st>>>(src, dst, nbytes, vec);
   return cudaGetLastError();
 }
 

@@ -13,8 +13,10 @@ struct ResultSet;
 struct WorkLists {
   int64_t *ovf;       // pairs whose int16 forward pass crossed the ceiling
   int *ovf_count;
-  int64_t *wide;      // pairs whose reverse band is wider than the banded kernel handles
+  int64_t *wide;      // pairs whose reverse band is wider than the banded kernels handle
   int *wide_count;
+  int64_t *esc1, *esc2;  // escalation lists between the banded begin kernels (16 -> 32 -> 64 cells)
+  int *esc1_count, *esc2_count;
   int64_t cap;        // capacity of each list
 };
 
@@ -26,16 +28,15 @@ struct FwdConfig {
   int pad;            // leading PAD entries
   int grid;           // blocks (grid-stride over pairs)
   size_t smem;        // dynamic shared memory bytes
+  bool keyed;         // int16 forward uses the keyed engine (mhsw_engine16.cuh)
 };
 
 // Upper bound of B length the forward kernels accept (shared-memory code buffer).
-constexpr int kMaxB = 65536;
-// Widest reverse band handled by the banded begin kernel; wider ones use the wavefront.
-constexpr int kBandMax = 256;
+constexpr int kMaxB = 65000;
 
 // Chooses K/G/grid/smem for a forward launch over pairs whose A (rows) lengths are at
 // most max_a and B lengths at most max_b.  wide32 selects the int32 engine.
-cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg);
+cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg, bool keyed = false);
 
 // Bytes of strip scratch a forward launch needs (0 when A fits one strip).
 size_t forward_scratch_bytes(const FwdConfig &cfg, int max_a, int max_b, bool wide32);
@@ -46,10 +47,19 @@ cudaError_t launch_forward(const FwdConfig &cfg, bool wide32, const PairSet &ps,
                            const Scoring &sc, const int64_t *list, const int *list_count, int ceiling,
                            void *scratch, const WorkLists &wl, cudaStream_t st);
 
-// Begin pass: banded thread-per-pair kernel for all pairs, then the wavefront kernel on
-// reversed prefixes for the pairs listed in wl.wide.
+// True when the keyed int16 engine (mhsw_engine16.cuh) can run this scoring: every
+// substitution score plus the gap-open penalty is non-negative.
+bool keyed_scoring(const Scoring &sc);
+
+// Begin pass: banded thread-per-pair kernels (bands of up to 16, 32, 64 cells, each
+// escalating to the next), then the wavefront kernel on reversed prefixes for the pairs
+// left in wl.wide.  order (may be null) is the pair order of the first kernel.
 cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, const Scoring &sc, int max_a,
-                           int max_b, void *scratch, size_t scratch_bytes, const WorkLists &wl, cudaStream_t st);
+                           int max_b, void *scratch, size_t scratch_bytes, const WorkLists &wl, cudaStream_t st,
+                           const uint32_t *order);
+
+// Raw bytes -> base codes (0..4) for one arena.
+cudaError_t launch_translate(const char *src, uint8_t *dst, int64_t nbytes, cudaStream_t st);
 
 // Clears the device work-list counters.
 cudaError_t reset_lists(const WorkLists &wl, cudaStream_t st);

@@ -26,6 +26,10 @@ struct PairSet {  // device pointers; A = SSW ref (rows), B = SSW query (columns
   const int64_t *b_off;
   const int32_t *b_len;
   int64_t n;
+  // Base codes (0..4, SSW's translation) at the same offsets as the raw bytes; filled
+  // once per batch by the translation kernel and read by every alignment kernel.
+  const uint8_t *a_code;
+  const uint8_t *b_code;
 };
 
 struct ResultSet {  // device pointers, one entry per pair

@@ -76,6 +76,8 @@ class PairsT(C.Structure):
         ("max_a_len", C.c_int32),
         ("max_b_len", C.c_int32),
         ("cells", C.c_double),
+        ("a_bytes", C.c_int64),
+        ("b_bytes", C.c_int64),
     ]
 
 
@@ -355,7 +357,7 @@ class Pairs:
             if arr.dtype != dt or not arr.flags.c_contiguous:
                 raise RuntimeError("Pairs arrays must be contiguous with dtypes uint8/int64/int32")
         return PairsT(self.a_seq.ctypes.data, self.a_off.ctypes.data, self.a_len.ctypes.data,
-                      self.b_seq.ctypes.data, self.b_off.ctypes.data, self.b_len.ctypes.data, self.n, 0, 0, 0.0)
+                      self.b_seq.ctypes.data, self.b_off.ctypes.data, self.b_len.ctypes.data, self.n, 0, 0, 0.0, 0, 0)
 
     def a(self, i: int) -> bytes:
         o = int(self.a_off[i])
@@ -417,7 +419,9 @@ class DevicePairs:
     max_a_len: int = 0
     max_b_len: int = 0
     cells: float = 0.0
+    a_bytes: int = 0
+    b_bytes: int = 0
 
     def c_struct(self) -> PairsT:
         return PairsT(self.a_seq, self.a_off, self.a_len, self.b_seq, self.b_off, self.b_len, self.n,
-                      self.max_a_len, self.max_b_len, self.cells)
+                      self.max_a_len, self.max_b_len, self.cells, self.a_bytes, self.b_bytes)
