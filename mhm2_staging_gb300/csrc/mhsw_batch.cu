@@ -69,11 +69,11 @@ __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, S
   const int lane = threadIdx.x % G;
   const unsigned gmask = group_mask_b(G);
   constexpr size_t kProf = group_prof16_bytes<8, G>();
-  unsigned char *gbase = smem + (size_t)grp * (kProf + (size_t)bcap);
+  unsigned char *gbase = smem + (size_t)grp * kProf;  // keyed engine: profile table only
   GroupSmem gs;
   gs.prof = reinterpret_cast<uint32_t *>(gbase);
   gs.prof_lanes = G;
-  gs.bcodes = gbase + kProf;
+  gs.bcodes = nullptr;
   gs.pad = pad;
   gs.bcap = bcap;
   const int64_t gid = (int64_t)blockIdx.x * gpb + grp;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, S
       }
       continue;
     }
-    const bool too_long = (N > bcap - pad - 2 * G) || (bucket == kBucketStrip && (bnd == nullptr || N > scratch_stride));
+    const bool too_long = (N > kMaxB) || (bucket == kBucketStrip && (bnd == nullptr || N > scratch_stride));
     if (M <= 0 || N <= 0 || too_long) {
       if (lane == 0) {
         rs.score[p] = 0;
@@ -201,7 +201,7 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     bs.err = "B longer than the kernel limit";
     return 1;
   }
-  const size_t per_group = group_prof16_bytes<8, kGB>() + (size_t)bcap;
+  const size_t per_group = group_prof16_bytes<8, kGB>();
   auto kern = k_fwd_persist<kGB>;
 
   // keys + sort (the order is reused by every tuning trial)

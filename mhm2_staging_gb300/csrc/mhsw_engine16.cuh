@@ -21,7 +21,10 @@
 //     SSW (ssw_core.cpp:474-506).  Keys need H < 4096, so this engine flags pairs whose
 //     score reaches the ceiling (at most kCeiling16) for the int32 engine.
 //  3. The profile table holds separate low-half and high-half words, loaded as 128-bit
-//     vectors; the high words loaded at step t serve the high half at step t+1.
+//     vectors; the high words loaded at step t serve the high half at step t+1 (the
+//     step loop is unrolled by two so the two word sets alternate registers).
+//  4. B codes are read from global memory (prefetched a step ahead) instead of being
+//     staged in shared memory, so a group's shared memory is its profile table only.
 #pragma once
 #include "mhsw_engine.cuh"
 
@@ -48,26 +51,78 @@ __device__ __forceinline__ uint32_t sign_mask16(uint32_t x) {
   return r;
 }
 
+// One wavefront step of the keyed engine for one lane.  W holds this step's profile
+// words (lo words used now), Phi the high words of the previous step; both are
+// register arrays of the caller, alternated between steps so no copies are needed.
 template <int K, int G>
-__device__ void sweep16(const SeqView &A, const SeqView &B, const Scoring &sc, const GroupSmem &gs, int lane,
-                        unsigned gmask, V16::Pay *bnd, int ceiling, SweepOut &out) {
+struct Step16 {
   using L = Prof16<K>;
+  __device__ static __forceinline__ void run(int t, uint32_t z, const uint32_t (&W)[L::kWords],
+                                             const uint32_t (&Phi)[L::kWords], uint32_t (&H)[K], uint32_t (&F)[K],
+                                             uint32_t &Hlast, uint32_t &Ecout, uint32_t &HtopPrev, uint32_t &Zout,
+                                             uint32_t &Kl, uint32_t &Jp, uint32_t NGE, uint32_t NGO) {
+    uint32_t Ev = __byte_perm(z, Ecout, 0x5432);  // lo: from the left lane, hi: own lo half
+    const uint32_t Htop = __byte_perm(z, Hlast, 0x5410);
+    uint32_t Hd = HtopPrev;
+    HtopPrev = Htop;
+    uint32_t key[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const uint32_t Q = Hd + W[k] + Phi[K + k];  // halves never carry: all terms >= 0, sum < 2^15
+      const uint32_t m = __vimax3_s16x2(Q, Ev, F[k]);
+      const uint32_t Hn = __viaddmax_s16x2_relu(m, NGO, 0u);
+      Ev = __viaddmax_s16x2(Ev, NGE, Hn);
+      F[k] = __viaddmax_s16x2(F[k], NGE, Hn);
+      Hd = H[k];
+      H[k] = Hn;
+      key[k] = Hn * 8u + (uint32_t)(7 - k) * 0x00010001u;
+    }
+    uint32_t km = key[0];
+#pragma unroll
+    for (int k = 1; k + 1 < K; k += 2) km = __vimax3_s16x2(km, key[k], key[k + 1]);
+    if ((K % 2) == 0) km = __vimax_s16x2_relu(km, key[K - 1]);
+    Zout = __byte_perm(H[K - 1], Ev, 0x7632);
+    Hlast = H[K - 1];
+    Ecout = Ev;
+    // running key per half; record the step where it strictly grows
+    const uint32_t Kn = __vimax_s16x2_relu(Kl, km);
+    const uint32_t msk = sign_mask16(Kn - Kl + 0x7fff7fffu);
+    const uint32_t tt = (uint32_t)t * 0x00010001u;
+    Jp = (msk & tt) | (~msk & Jp);
+    Kl = Kn;
+  }
+  __device__ static __forceinline__ void load(const uint4 *tab, int c, int lane, uint32_t (&W)[L::kWords]) {
+#pragma unroll
+    for (int q = 0; q < L::kNQ; q++) {
+      const uint4 v = tab[(c * L::kNQ + q) * G + lane];
+      W[4 * q + 0] = v.x;
+      W[4 * q + 1] = v.y;
+      W[4 * q + 2] = v.z;
+      W[4 * q + 3] = v.w;
+    }
+  }
+};
+
+// Forward sweep of one pair with the keyed engine.  B is read directly from its code
+// array in global memory (one byte per lane per step, prefetched a step ahead); the
+// shared memory of the group holds only the profile table.  A must be a forward view.
+template <int K, int G, bool MULTI>
+__device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &sc, const GroupSmem &gs, int lane,
+                             unsigned gmask, V16::Pay *bnd, int ceiling, SweepOut &out) {
+  using L = Prof16<K>;
+  using ST = Step16<K, G>;
   constexpr int RS = 2 * K * G;
   const int M = A.len, N = B.len;
   const uint32_t NGE = V16::splat(-sc.gap_extend);
   const uint32_t NGO = V16::splat(-sc.gap_open);
-
-  // B codes into shared memory: bcodes[pad + j] for j in [-pad, N + 2G); PAD outside [0, N).
-  const int fill = gs.pad + N + 2 * G < gs.bcap ? gs.pad + N + 2 * G : gs.bcap;
-  for (int x = lane; x < fill; x += G) gs.bcodes[x] = (uint8_t)B.code(x - gs.pad);
-  __syncwarp(gmask);
+  const uint8_t *bg = B.base;
 
   unsigned long long best = 0ull;
   int overflow = 0;
   const int nstrips = (M + RS - 1) / RS;
   const int T_end = N + 2 * G - 1;
   const uint4 *tab = reinterpret_cast<const uint4 *>(gs.prof);
-  const uint8_t *bc = gs.bcodes + gs.pad - 2 * lane;  // bc[t] = code of this lane's lo column at step t
+  const uint32_t zmask = lane == 0 ? 0u : 0xffffffffu;  // lane 0 sees the zero top boundary
 
   for (int s = 0; s < nstrips; s++) {
     const int row0 = s * RS + lane * 2 * K;
@@ -91,73 +146,59 @@ __device__ void sweep16(const SeqView &A, const SeqView &B, const Scoring &sc, c
     }
     __syncwarp(gmask);
 
-    uint32_t H[K], F[K], Phi[K];
+    uint32_t H[K], F[K], WA[L::kWords], WB[L::kWords];
 #pragma unroll
     for (int k = 0; k < K; k++) {
       H[k] = 0u;
-      F[k] = 0u;    // F^ = F + gO with F = -gO before column 0
-      Phi[k] = 0u;  // hi words of the PAD column before column 0 (score -gO, biased 0)
+      F[k] = 0u;  // F^ = F + gO with F = -gO before column 0
     }
+#pragma unroll
+    for (int w = 0; w < L::kWords; w++) WB[w] = 0u;  // the PAD column before column 0 (biased score 0)
     uint32_t Hlast = 0u, Ecout = 0u, HtopPrev = 0u;
     uint32_t Zout = 0u;  // (lo: H of the hi-last row, hi: E^ below it)
     uint32_t Kl = 0u;    // running key per half
     uint32_t Jp = 0u;    // step of the last strict increase of Kl, per half
+    constexpr bool multi = MULTI;
     const bool first_strip = (s == 0);
     const bool last_strip = (s == nstrips - 1);
+    const int j0 = -2 * lane;  // lo column at step 0
+    int cnext = (j0 >= 0 && j0 < N) ? (int)bg[j0] : kCodePad;
 
-    for (int t = 0; t < T_end; t++) {
-      const int c = bc[t];
-      uint32_t w[L::kWords];
-#pragma unroll
-      for (int q = 0; q < L::kNQ; q++) {
-        const uint4 v = tab[(c * L::kNQ + q) * G + lane];
-        w[4 * q + 0] = v.x;
-        w[4 * q + 1] = v.y;
-        w[4 * q + 2] = v.z;
-        w[4 * q + 3] = v.w;
-      }
-      uint32_t z = __shfl_up_sync(gmask, Zout, 1, G);
-      if (lane == 0) {
-        z = 0u;
-        if (!first_strip) {
-          const int j = t;
-          if (j < N) z = bnd[j];
-        }
-      }
-      uint32_t Ev = __byte_perm(z, Ecout, 0x5432);        // lo: from the left lane, hi: own lo half
-      const uint32_t Htop = __byte_perm(z, Hlast, 0x5410);
-      uint32_t Hd = HtopPrev;
-      HtopPrev = Htop;
-      uint32_t key[K];
-#pragma unroll
-      for (int k = 0; k < K; k++) {
-        const uint32_t Q = Hd + w[k] + Phi[k];  // halves never carry: all terms >= 0, sum < 2^15
-        const uint32_t m = __vimax3_s16x2(Q, Ev, F[k]);
-        const uint32_t Hn = __viaddmax_s16x2_relu(m, NGO, 0u);
-        Ev = __viaddmax_s16x2(Ev, NGE, Hn);
-        F[k] = __viaddmax_s16x2(F[k], NGE, Hn);
-        Hd = H[k];
-        H[k] = Hn;
-        key[k] = Hn * 8u + (uint32_t)(7 - k) * 0x00010001u;
-        Phi[k] = w[K + k];
-      }
-      uint32_t km = key[0];
-#pragma unroll
-      for (int k = 1; k + 1 < K; k += 2) km = __vimax3_s16x2(km, key[k], key[k + 1]);
-      if ((K % 2) == 0) km = __vimax_s16x2_relu(km, key[K - 1]);
-      Zout = __byte_perm(H[K - 1], Ev, 0x7632);
-      Hlast = H[K - 1];
-      Ecout = Ev;
-      // running key per half; record the step where it strictly grows
-      const uint32_t Kn = __vimax_s16x2_relu(Kl, km);
-      const uint32_t msk = sign_mask16(Kn - Kl + 0x7fff7fffu);
-      const uint32_t tt = (uint32_t)t * 0x00010001u;
-      Jp = (msk & tt) | (~msk & Jp);
-      Kl = Kn;
-      if (!last_strip && lane == G - 1) {
+    auto top = [&](int t, uint32_t zs) -> uint32_t {
+      uint32_t z = zs & zmask;
+      if (multi && lane == 0 && !first_strip && t < N) z = bnd[t];
+      return z;
+    };
+    auto out_bnd = [&](int t) {
+      if (multi && !last_strip && lane == G - 1) {
         const int jh = t - 2 * lane - 1;  // hi-half column of the last lane
         if (jh >= 0 && jh < N) bnd[jh] = Zout;
       }
+    };
+    int t = 0;
+    for (; t + 1 < T_end; t += 2) {
+      // even step: profile words into WA, previous high words in WB
+      int c = cnext;
+      int jn = t + 1 + j0;
+      cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodePad;
+      ST::load(tab, c, lane, WA);
+      uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
+      ST::run(t, z, WA, WB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO);
+      out_bnd(t);
+      // odd step: into WB, previous high words in WA
+      c = cnext;
+      jn = t + 2 + j0;
+      cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodePad;
+      ST::load(tab, c, lane, WB);
+      z = top(t + 1, __shfl_up_sync(gmask, Zout, 1, G));
+      ST::run(t + 1, z, WB, WA, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO);
+      out_bnd(t + 1);
+    }
+    if (t < T_end) {
+      ST::load(tab, cnext, lane, WA);
+      const uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
+      ST::run(t, z, WA, WB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO);
+      out_bnd(t);
     }
 
     // Decode the two halves' keys into (value, row, column) and reduce over the group.
@@ -189,6 +230,15 @@ __device__ void sweep16(const SeqView &A, const SeqView &B, const Scoring &sc, c
   }
   out.key = best;
   out.overflow = overflow;
+}
+
+template <int K, int G>
+__device__ __forceinline__ void sweep16(const SeqView &A, const SeqView &B, const Scoring &sc, const GroupSmem &gs,
+                                        int lane, unsigned gmask, V16::Pay *bnd, int ceiling, SweepOut &out) {
+  if (A.len > 2 * K * G)
+    sweep16_impl<K, G, true>(A, B, sc, gs, lane, gmask, bnd, ceiling, out);
+  else
+    sweep16_impl<K, G, false>(A, B, sc, gs, lane, gmask, bnd, ceiling, out);
 }
 
 }  // namespace mhsw

@@ -111,11 +111,11 @@ __global__ void __launch_bounds__(256) k_fwd16(PairSet ps, ResultSet rs, Scoring
   const int lane = threadIdx.x % G;
   const unsigned gmask = group_mask(G);
   constexpr size_t kProf = group_prof16_bytes<K, G>();
-  unsigned char *gbase = smem + (size_t)grp * (kProf + (size_t)bcap);
+  unsigned char *gbase = smem + (size_t)grp * kProf;  // keyed engine: profile table only
   GroupSmem gs;
   gs.prof = reinterpret_cast<uint32_t *>(gbase);
   gs.prof_lanes = G;
-  gs.bcodes = gbase + kProf;
+  gs.bcodes = nullptr;
   gs.pad = pad;
   gs.bcap = bcap;
   constexpr int RS = 2 * K * G;
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) k_fwd16(PairSet ps, ResultSet rs, Scoring
   V16::Pay *bnd = scratch ? scratch + gid * (int64_t)scratch_stride : nullptr;
   for (int64_t p = gid; p < ps.n; p += gstride) {
     const int M = ps.a_len[p], N = ps.b_len[p];
-    const bool too_long = (N > bcap - pad - 2 * G) || (M > RS && (bnd == nullptr || N > scratch_stride));
+    const bool too_long = (N > kMaxB) || (M > RS && (bnd == nullptr || N > scratch_stride));
     if (M <= 0 || N <= 0 || too_long) {
       if (lane == 0) {
         rs.score[p] = 0;
@@ -520,7 +520,9 @@ cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfi
   if (max_b > kMaxB) return cudaErrorInvalidValue;
   c.bcap = ((c.pad + max_b + 2 * kG) + 15) / 16 * 16;
   const size_t budget = 100 * 1024;  // keep two blocks per SM possible
-  const size_t per_group = ((keyed && !wide32) ? group_prof16_rt(c.K) : group_prof_rt(wide32, c.K)) + (size_t)c.bcap;
+  // the keyed engine reads B from global memory: its group needs the profile table only
+  const size_t per_group =
+      (keyed && !wide32) ? group_prof16_rt(c.K) : group_prof_rt(wide32, c.K) + (size_t)c.bcap;
   int gpb = 8;
   while (gpb > 1 && (size_t)gpb * per_group > budget) gpb /= 2;
   c.groups_per_block = gpb;
