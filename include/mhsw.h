@@ -181,6 +181,10 @@ int mhsw_last_timing(mhsw_driver *drv, mhsw_timing *out);
  * the whole GPU, *sm_hz = SM cycles per second seen by the probe.  Basis of the
  * cell-update roofline. */
 int mhsw_probe_dpx_rate(int device, double *ops_per_s, double *sm_hz);
+/* Throughput of one instruction form (lane operations per second, all SMs busy):
+ * op 0 __viaddmax_s16x2, 1 __vimax3_s16x2, 2 __viaddmax_s16x2_relu,
+ * 3 __vimax_s16x2_relu, 4 three-operand integer add, 5 integer multiply-add. */
+int mhsw_probe_op_rate(int device, int op, double *ops_per_s);
 
 #ifdef __cplusplus
 }

@@ -22,23 +22,19 @@ namespace mhsw {
 
 namespace {
 
-constexpr int kGB = 16;
 constexpr int kKeyShift = 17;
-constexpr int kBucketStrip = 6;  // A longer than one K=8 strip
-constexpr int kBucketWide = 7;   // straight to int32
-constexpr int kInt16Capacity = kCeiling16;  // keyed int16 engine
+// Buckets: 0..3 = A up to 64/96/128/160 rows (8-lane groups, K = 4/6/8/10),
+// 4/5 = up to 192/256 rows (16-lane groups, K = 6/8), 6 = longer A (K = 8 strips),
+// 7 = could exceed the int16 keys: straight to the int32 list.
+constexpr int kBucketFirstLong = 4;
+constexpr int kBucketStrip = 6;
+constexpr int kBucketWide = 7;
 
 __device__ __forceinline__ int bucket_of(int M, int N, const Scoring &sc) {
+  const int K = keyed_k_for_rows(M);
   const long long bound = (long long)(M < N ? M : N) * sc.match;
-  if (bound > kInt16Capacity) return kBucketWide;
-  if (M > 2 * 8 * kGB) return kBucketStrip;
-  const int need = (M + 2 * kGB - 1) / (2 * kGB);
-  if (need <= 2) return 0;
-  if (need <= 3) return 1;
-  if (need <= 4) return 2;
-  if (need <= 5) return 3;
-  if (need <= 6) return 4;
-  return 5;
+  if (bound > keyed_cap(K)) return kBucketWide;
+  return M <= 64 ? 0 : M <= 96 ? 1 : M <= 128 ? 2 : M <= 160 ? 3 : M <= 192 ? 4 : M <= 256 ? 5 : kBucketStrip;
 }
 
 __global__ void k_keys(PairSet ps, Scoring sc, uint32_t *keys, uint32_t *idx) {
@@ -57,18 +53,34 @@ __device__ __forceinline__ unsigned group_mask_b(int G) {
   return ((1u << G) - 1u) << ((lane32 / G) * G);
 }
 
+// First sorted item of the long-read buckets (the sorted keys are ascending).
+__global__ void k_split(const uint32_t *__restrict__ keys, int64_t n, int *split) {
+  const uint32_t first = (uint32_t)kBucketFirstLong << kKeyShift;
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) / 2;
+    if (keys[mid] < first) lo = mid + 1;
+    else hi = mid;
+  }
+  *split = (int)lo;
+}
+
+// Persistent forward kernel over one range of the sorted pair order: 8-lane groups for
+// the short-read buckets (items [0, split)), 16-lane groups for the rest ([split, n)).
+// A group claims its next pair from the range's atomic counter.
 template <int G>
 __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, Scoring sc,
                                                      const uint32_t *__restrict__ keys,
                                                      const uint32_t *__restrict__ order, int64_t n, int *queue,
-                                                     int ceiling, WorkLists wl, int pad, int bcap, V16::Pay *scratch,
-                                                     int scratch_stride) {
+                                                     const int *split, int ceiling, WorkLists wl, int pad, int bcap,
+                                                     V16::Pay *scratch, int scratch_stride) {
+  constexpr bool kShort = (G == kGKShort);
   extern __shared__ __align__(16) unsigned char smem[];
   const int gpb = blockDim.x / G;
   const int grp = threadIdx.x / G;
   const int lane = threadIdx.x % G;
   const unsigned gmask = group_mask_b(G);
-  constexpr size_t kProf = group_prof16_bytes<8, G>();
+  constexpr size_t kProf = kShort ? group_prof16_bytes<10, G>() : group_prof16_bytes<8, G>();
   unsigned char *gbase = smem + (size_t)grp * kProf;  // keyed engine: profile table only
   GroupSmem gs;
   gs.prof = reinterpret_cast<uint32_t *>(gbase);
@@ -78,12 +90,16 @@ __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, S
   gs.bcap = bcap;
   const int64_t gid = (int64_t)blockIdx.x * gpb + grp;
   V16::Pay *bnd = scratch ? scratch + gid * (int64_t)scratch_stride : nullptr;
+  const int64_t lo = kShort ? 0 : *split;
+  const int64_t hi = kShort ? *split : n;
+  int *counter = queue + (kShort ? 0 : 1);
 
   for (;;) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(queue, 1);
-    item = __shfl_sync(gmask, item, 0, G);
-    if (item >= n) break;
+    int claim = 0;
+    if (lane == 0) claim = atomicAdd(counter, 1);
+    claim = __shfl_sync(gmask, claim, 0, G);
+    const int64_t item = lo + claim;
+    if (item >= hi) break;
     const uint32_t key = keys[item];
     const int64_t p = order[item];
     const int bucket = (int)(key >> kKeyShift);
@@ -112,13 +128,16 @@ __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, S
     SeqView A{ps.a_code + ps.a_off[p], 1, M};
     SeqView B{ps.b_code + ps.b_off[p], 1, N};
     SweepOut so;
-    switch (bucket) {
-      case 0: sweep16<2, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      case 1: sweep16<3, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      case 2: sweep16<4, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      case 3: sweep16<5, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      case 4: sweep16<6, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-      default: sweep16<8, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+    if constexpr (kShort) {
+      switch (bucket) {
+        case 0: sweep16<4, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+        case 1: sweep16<6, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+        case 2: sweep16<8, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+        default: sweep16<10, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+      }
+    } else {
+      if (bucket == 4) sweep16<6, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so);
+      else sweep16<8, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so);
     }
     if (lane == 0) {
       const int S = key_value(so.key);
@@ -192,17 +211,20 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     bs.cap = c;
   }
   if (!bs.queue && (e = cudaMalloc(&bs.queue, sizeof(int) * 4))) return fail(e, "cudaMalloc queue");
+  // queue[0], queue[1]: claim counters of the short and long ranges; queue[2]: split item
 
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  const int pad = 2 * kGB;
-  const int bcap = ((pad + std::max(max_b, 1) + 2 * kGB) + 15) / 16 * 16;
   if (max_b > kMaxB) {
     bs.err = "B longer than the kernel limit";
     return 1;
   }
-  const size_t per_group = group_prof16_bytes<8, kGB>();
-  auto kern = k_fwd_persist<kGB>;
+  auto kshort = k_fwd_persist<kGKShort>;
+  auto klong = k_fwd_persist<kGKLong>;
+  const size_t prof_short = group_prof16_bytes<10, kGKShort>();
+  const size_t prof_long = group_prof16_bytes<8, kGKLong>();
+  const int pad = 2 * kGKLong;
+  const int bcap = ((pad + std::max(max_b, 1) + 2 * kGKLong) + 15) / 16 * 16;  // strip scratch stride
 
   // keys + sort (the order is reused by every tuning trial)
   {
@@ -213,30 +235,38 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     e = cub::DeviceRadixSort::SortPairs(bs.temp, tb, bs.keys_in, bs.keys_out, bs.idx_in, bs.idx_out, (int)n, 0, 20,
                                         st);
     if (e) return fail(e, "radix sort");
-    if (launches) *launches += 2 + 3;  // keys + cub's onesweep passes (approximate)
+    k_split<<<1, 1, 0, st>>>(bs.keys_out, n, bs.queue + 2);
+    if ((e = cudaGetLastError())) return fail(e, "split launch");
+    if (launches) *launches += 2 + 4;  // keys, split, and the radix sort's passes (approximate)
   }
 
   auto run = [&](const BatchShape &sh, float *ms) -> int {
-    const int gpb = sh.groups_per_block;
-    const size_t smem = (size_t)gpb * per_group;
-    if (smem > 48 * 1024) {
-      cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e2) return fail(e2, "smem attribute");
-    }
-    int occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, gpb * kGB, smem);
-    if (occ < 1) occ = 1;
-    int bps = sh.blocks_per_sm > 0 ? std::min(sh.blocks_per_sm, occ) : occ;
-    int grid = sms * bps;
+    const int threads = sh.groups_per_block * 8;  // block size: 8 groups of 8 lanes or 4 of 16, etc.
+    const int gpb_s = threads / kGKShort, gpb_l = threads / kGKLong;
+    const size_t smem_s = (size_t)gpb_s * prof_short, smem_l = (size_t)gpb_l * prof_long;
+    cudaError_t e2;
+    if (smem_s > 48 * 1024 && (e2 = cudaFuncSetAttribute(kshort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         (int)smem_s)))
+      return fail(e2, "smem attribute");
+    if (smem_l > 48 * 1024 && (e2 = cudaFuncSetAttribute(klong, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         (int)smem_l)))
+      return fail(e2, "smem attribute");
+    int occ_s = 0, occ_l = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, kshort, threads, smem_s);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_l, klong, threads, smem_l);
+    occ_s = std::max(occ_s, 1);
+    occ_l = std::max(occ_l, 1);
+    const int grid_s = sms * (sh.blocks_per_sm > 0 ? std::min(sh.blocks_per_sm, occ_s) : occ_s);
+    const int grid_l = sms * (sh.blocks_per_sm > 0 ? std::min(sh.blocks_per_sm, occ_l) : occ_l);
     V16::Pay *scr = nullptr;
-    int stride = bcap;
-    if (max_a > 2 * 8 * kGB) {
-      size_t need = (size_t)grid * gpb * (size_t)stride * sizeof(V16::Pay);
+    const int stride = bcap;
+    if (max_a > 2 * 8 * kGKLong) {
+      const size_t need = (size_t)grid_l * gpb_l * (size_t)stride * sizeof(V16::Pay);
       if (need > bs.scratch_bytes) {
         if (bs.scratch) cudaFree(bs.scratch);
         bs.scratch = nullptr;
         bs.scratch_bytes = 0;
-        cudaError_t e2 = cudaMalloc(&bs.scratch, need);
+        e2 = cudaMalloc(&bs.scratch, need);
         if (e2) return fail(e2, "cudaMalloc strip scratch");
         bs.scratch_bytes = need;
       }
@@ -248,13 +278,15 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
       cudaEventCreate(&t1);
       cudaEventRecord(t0, st);
     }
-    cudaMemsetAsync(bs.queue, 0, sizeof(int), st);
+    cudaMemsetAsync(bs.queue, 0, 2 * sizeof(int), st);
     cudaMemsetAsync(wl.ovf_count, 0, sizeof(int), st);
-    kern<<<grid, gpb * kGB, smem, st>>>(ps, rs, sc, bs.keys_out, bs.idx_out, n, bs.queue, ceiling, wl, pad, bcap, scr,
-                                        stride);
-    cudaError_t e2 = cudaGetLastError();
+    kshort<<<grid_s, threads, smem_s, st>>>(ps, rs, sc, bs.keys_out, bs.idx_out, n, bs.queue, bs.queue + 2, ceiling,
+                                             wl, pad, bcap, nullptr, stride);
+    klong<<<grid_l, threads, smem_l, st>>>(ps, rs, sc, bs.keys_out, bs.idx_out, n, bs.queue, bs.queue + 2, ceiling,
+                                           wl, pad, bcap, scr, stride);
+    e2 = cudaGetLastError();
     if (e2) return fail(e2, "persistent forward launch");
-    if (launches) *launches += 1;
+    if (launches) *launches += 2;
     if (ms) {
       cudaEventRecord(t1, st);
       cudaEventSynchronize(t1);
@@ -267,7 +299,8 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
 
   if (bs.autotune && !bs.tuned) {
     // Candidate launch shapes: groups per block x blocks per SM.
-    const BatchShape cands[] = {{2, 0}, {4, 0}, {8, 0}, {4, 2}, {8, 1}};
+    // shapes: block size (groups_per_block * 8 threads) x blocks per SM (0 = occupancy limit)
+    const BatchShape cands[] = {{8, 0}, {16, 0}, {32, 0}, {16, 2}, {32, 1}};
     float best = 1e30f;
     BatchShape pick = bs.shape;
     bs.tune_n = 0;

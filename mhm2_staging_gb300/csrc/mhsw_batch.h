@@ -12,8 +12,8 @@ struct WorkLists;
 
 // One tuned launch shape of the persistent kernel.
 struct BatchShape {
-  int groups_per_block = 4;
-  int blocks_per_sm = 0;  // 0 = occupancy maximum
+  int groups_per_block = 16;  // block size in units of 8 threads
+  int blocks_per_sm = 0;      // 0 = occupancy maximum
 };
 
 struct BatchState {

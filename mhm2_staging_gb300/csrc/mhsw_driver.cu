@@ -207,7 +207,7 @@ int ensure_results(mhsw_driver *d, int64_t n) {
   MHSW_CK(d->l_wide.reserve((size_t)n + 1), "cudaMalloc lists");
   MHSW_CK(d->l_esc1.reserve((size_t)n + 1), "cudaMalloc lists");
   MHSW_CK(d->l_esc2.reserve((size_t)n + 1), "cudaMalloc lists");
-  MHSW_CK(d->l_counts.reserve(4), "cudaMalloc lists");
+  MHSW_CK(d->l_counts.reserve(2 + mhsw::kEscLevels), "cudaMalloc lists");
   return MHSW_OK;
 }
 
@@ -230,8 +230,7 @@ mhsw::WorkLists work_lists(mhsw_driver *d, int64_t n) {
   wl.wide_count = d->l_counts.p + 1;
   wl.esc1 = d->l_esc1.p;
   wl.esc2 = d->l_esc2.p;
-  wl.esc1_count = d->l_counts.p + 2;
-  wl.esc2_count = d->l_counts.p + 3;
+  wl.esc_counts = d->l_counts.p + 2;
   wl.cap = n;
   return wl;
 }
@@ -325,7 +324,7 @@ int run_reverse(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, c
   MHSW_CK(mhsw::launch_reverse(d->device, ps, rs, d->sc, max_a, max_b, d->scratch.p,
                                d->scratch.p ? d->scratch.cap : 0, wl, d->st, order),
           "begin pass launch");
-  d->launches += 4;
+  d->launches += 8;
   return MHSW_OK;
 }
 

@@ -14,12 +14,13 @@
 //     engine.  PAD cells score -gO (biased 0), which keeps every value outside the
 //     matrix below the pair's maximum.
 //  2. The arg-max is tracked per lane half, not per row: each cell contributes the
-//     16-bit key H*8 + (7-k) (k = row within the half), so the maximum key is the
+//     16-bit key H*2^b + (2^b-1-k) (k = row within the half, b = 3 for up to 8 rows
+//     per half, else 4), so the maximum key is the
 //     largest score at the smallest row; the half's running key is kept with the step
 //     at which it last strictly grew.  Because steps are columns, that step is the
 //     first column at which that row reached that score -- the lexicographic rule of
-//     SSW (ssw_core.cpp:474-506).  Keys need H < 4096, so this engine flags pairs whose
-//     score reaches the ceiling (at most kCeiling16) for the int32 engine.
+//     SSW (ssw_core.cpp:474-506).  Keys need H < 2^(15-b), so this engine flags pairs
+//     whose score reaches the ceiling (at most KeyBits::kCap) for the int32 engine.
 //  3. The profile table holds separate low-half and high-half words, loaded as 128-bit
 //     vectors; the high words loaded at step t serve the high half at step t+1 (the
 //     step loop is unrolled by two so the two word sets alternate registers).
@@ -30,18 +31,35 @@
 
 namespace mhsw {
 
-constexpr int kCeiling16 = 4000;  // largest score the keyed int16 engine accepts
+constexpr int kCeiling16 = 4000;  // largest score the keyed int16 engine accepts (8 or fewer rows per half)
+// Lane groups of the keyed kernels: 8 lanes per pair for A up to 160 rows (K = 4, 6, 8, 10
+// rows-pairs per lane), 16 lanes for longer A (K = 6, 8; strips of 256 rows beyond).
+constexpr int kGKShort = 8;
+constexpr int kGKLong = 16;
+constexpr int kShortRows = 160;
+__host__ __device__ constexpr int keyed_g_for_rows(int rows) { return rows <= kShortRows ? kGKShort : kGKLong; }
+__host__ __device__ constexpr int keyed_k_for_rows(int rows) {
+  return rows <= 64 ? 4 : rows <= 96 ? 6 : rows <= 128 ? 8 : rows <= 160 ? 10 : rows <= 192 ? 6 : 8;
+}
+__host__ __device__ constexpr int keyed_cap(int K) { return K <= 8 ? (1 << 12) - 64 : (1 << 11) - 64; }
 
 template <int K>
 struct Prof16 {
-  static constexpr int kWords = ((2 * K + 3) / 4) * 4;  // lo words [0,K), hi words [K,2K), padded
-  static constexpr int kNQ = kWords / 4;
+  static constexpr int kNQh = (K + 3) / 4;   // 128-bit vectors per half (lo words, then hi words)
+  static constexpr int kNQ = 2 * kNQh;
+  static constexpr int kWh = 4 * kNQh;       // words per half, padded
   __host__ __device__ static constexpr size_t bytes(int lanes) { return (size_t)kNumCodes * kNQ * lanes * 16; }
 };
 
 template <int KMAX, int G>
 __host__ __device__ constexpr size_t group_prof16_bytes() {
   return Prof16<KMAX>::bytes(G);
+}
+
+__device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t r;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(c));
+  return r;
 }
 
 __device__ __forceinline__ uint32_t sign_mask16(uint32_t x) {
@@ -54,13 +72,23 @@ __device__ __forceinline__ uint32_t sign_mask16(uint32_t x) {
 // One wavefront step of the keyed engine for one lane.  W holds this step's profile
 // words (lo words used now), Phi the high words of the previous step; both are
 // register arrays of the caller, alternated between steps so no copies are needed.
+// Arg-max key of a cell: H << kKeyBits | (kKeyMask - k), k = row within the lane half.
+template <int K>
+struct KeyBits {
+  static constexpr int kBits = K <= 8 ? 3 : 4;
+  static constexpr uint32_t kMask = (1u << kBits) - 1u;
+  static constexpr int kCap = (1 << (15 - kBits)) - 64;  // largest score a key holds, with margin
+};
+
 template <int K, int G>
 struct Step16 {
   using L = Prof16<K>;
-  __device__ static __forceinline__ void run(int t, uint32_t z, const uint32_t (&W)[L::kWords],
-                                             const uint32_t (&Phi)[L::kWords], uint32_t (&H)[K], uint32_t (&F)[K],
+  static constexpr uint32_t kKeyMask = KeyBits<K>::kMask;
+  __device__ static __forceinline__ void run(int t, uint32_t z, const uint32_t (&Wlo)[L::kWh],
+                                             const uint32_t (&Phi)[L::kWh], uint32_t (&H)[K], uint32_t (&F)[K],
                                              uint32_t &Hlast, uint32_t &Ecout, uint32_t &HtopPrev, uint32_t &Zout,
-                                             uint32_t &Kl, uint32_t &Jp, uint32_t NGE, uint32_t NGO) {
+                                             uint32_t &Kl, uint32_t &Jp, uint32_t NGE, uint32_t NGO, uint32_t one,
+                                             uint32_t eight) {
     uint32_t Ev = __byte_perm(z, Ecout, 0x5432);  // lo: from the left lane, hi: own lo half
     const uint32_t Htop = __byte_perm(z, Hlast, 0x5410);
     uint32_t Hd = HtopPrev;
@@ -68,14 +96,16 @@ struct Step16 {
     uint32_t key[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
-      const uint32_t Q = Hd + W[k] + Phi[K + k];  // halves never carry: all terms >= 0, sum < 2^15
+      // halves never carry: all terms >= 0, sum < 2^15.  Written as multiply-adds by a
+      // runtime 1 so they issue on the FMA pipe, not the integer ALU pipe the DP saturates.
+      const uint32_t Q = mad_u32(mad_u32(Hd, one, Wlo[k]), one, Phi[k]);
       const uint32_t m = __vimax3_s16x2(Q, Ev, F[k]);
       const uint32_t Hn = __viaddmax_s16x2_relu(m, NGO, 0u);
       Ev = __viaddmax_s16x2(Ev, NGE, Hn);
       F[k] = __viaddmax_s16x2(F[k], NGE, Hn);
       Hd = H[k];
       H[k] = Hn;
-      key[k] = Hn * 8u + (uint32_t)(7 - k) * 0x00010001u;
+      key[k] = mad_u32(Hn, eight, (uint32_t)(kKeyMask - k) * 0x00010001u);
     }
     uint32_t km = key[0];
 #pragma unroll
@@ -91,10 +121,22 @@ struct Step16 {
     Jp = (msk & tt) | (~msk & Jp);
     Kl = Kn;
   }
-  __device__ static __forceinline__ void load(const uint4 *tab, int c, int lane, uint32_t (&W)[L::kWords]) {
+  // lo words of code c (used at this step)
+  __device__ static __forceinline__ void load_lo(const uint4 *tab, int c, int lane, uint32_t (&W)[L::kWh]) {
 #pragma unroll
-    for (int q = 0; q < L::kNQ; q++) {
+    for (int q = 0; q < L::kNQh; q++) {
       const uint4 v = tab[(c * L::kNQ + q) * G + lane];
+      W[4 * q + 0] = v.x;
+      W[4 * q + 1] = v.y;
+      W[4 * q + 2] = v.z;
+      W[4 * q + 3] = v.w;
+    }
+  }
+  // hi words of code c (used at the next step by the high half)
+  __device__ static __forceinline__ void load_hi(const uint4 *tab, int c, int lane, uint32_t (&W)[L::kWh]) {
+#pragma unroll
+    for (int q = 0; q < L::kNQh; q++) {
+      const uint4 v = tab[(c * L::kNQ + L::kNQh + q) * G + lane];
       W[4 * q + 0] = v.x;
       W[4 * q + 1] = v.y;
       W[4 * q + 2] = v.z;
@@ -112,10 +154,13 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
   using L = Prof16<K>;
   using ST = Step16<K, G>;
   constexpr int RS = 2 * K * G;
+  constexpr int KB = KeyBits<K>::kBits;
+  constexpr uint32_t KMASK = KeyBits<K>::kMask;
   const int M = A.len, N = B.len;
   const uint32_t NGE = V16::splat(-sc.gap_extend);
   const uint32_t NGO = V16::splat(-sc.gap_open);
   const uint8_t *bg = B.base;
+  if (ceiling > KeyBits<K>::kCap) ceiling = KeyBits<K>::kCap;
 
   unsigned long long best = 0ull;
   int overflow = 0;
@@ -123,6 +168,9 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
   const int T_end = N + 2 * G - 1;
   const uint4 *tab = reinterpret_cast<const uint4 *>(gs.prof);
   const uint32_t zmask = lane == 0 ? 0u : 0xffffffffu;  // lane 0 sees the zero top boundary
+  // 1 and 2^KB as values the compiler cannot fold (gs.pad is a launch argument >= 0)
+  const uint32_t one = (uint32_t)(gs.pad >> 30) + 1u;
+  const uint32_t scale = one << KB;
 
   for (int s = 0; s < nstrips; s++) {
     const int row0 = s * RS + lane * 2 * K;
@@ -132,33 +180,32 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
       uint32_t *tw = gs.prof;
       for (int c = 0; c < kNumCodes; c++) {
 #pragma unroll
-        for (int w = 0; w < L::kWords; w++) {
-          uint32_t v = 0;
-          if (w < K) {
-            v = (uint32_t)(sub_score(A.code(row0 + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu;
-          } else if (w < 2 * K) {
-            v = ((uint32_t)(sub_score(A.code(row0 + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu) << 16;
-          }
+        for (int w = 0; w < L::kWh; w++) {
+          const uint32_t vlo =
+              w < K ? (uint32_t)(sub_score(A.code(row0 + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu : 0u;
+          const uint32_t vhi =
+              w < K ? ((uint32_t)(sub_score(A.code(row0 + K + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu) << 16
+                    : 0u;
           const int q = w / 4, r = w % 4;
-          tw[((c * L::kNQ + q) * G + lane) * 4 + r] = v;
+          tw[((c * L::kNQ + q) * G + lane) * 4 + r] = vlo;
+          tw[((c * L::kNQ + L::kNQh + q) * G + lane) * 4 + r] = vhi;
         }
       }
     }
     __syncwarp(gmask);
 
-    uint32_t H[K], F[K], WA[L::kWords], WB[L::kWords];
+    uint32_t H[K], F[K], Wlo[L::kWh], HA[L::kWh], HB[L::kWh];
 #pragma unroll
     for (int k = 0; k < K; k++) {
       H[k] = 0u;
       F[k] = 0u;  // F^ = F + gO with F = -gO before column 0
     }
 #pragma unroll
-    for (int w = 0; w < L::kWords; w++) WB[w] = 0u;  // the PAD column before column 0 (biased score 0)
+    for (int w = 0; w < L::kWh; w++) HB[w] = 0u;  // hi words of the PAD column before column 0 (biased 0)
     uint32_t Hlast = 0u, Ecout = 0u, HtopPrev = 0u;
     uint32_t Zout = 0u;  // (lo: H of the hi-last row, hi: E^ below it)
     uint32_t Kl = 0u;    // running key per half
     uint32_t Jp = 0u;    // step of the last strict increase of Kl, per half
-    constexpr bool multi = MULTI;
     const bool first_strip = (s == 0);
     const bool last_strip = (s == nstrips - 1);
     const int j0 = -2 * lane;  // lo column at step 0
@@ -166,38 +213,40 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
 
     auto top = [&](int t, uint32_t zs) -> uint32_t {
       uint32_t z = zs & zmask;
-      if (multi && lane == 0 && !first_strip && t < N) z = bnd[t];
+      if (MULTI && lane == 0 && !first_strip && t < N) z = bnd[t];
       return z;
     };
     auto out_bnd = [&](int t) {
-      if (multi && !last_strip && lane == G - 1) {
+      if (MULTI && !last_strip && lane == G - 1) {
         const int jh = t - 2 * lane - 1;  // hi-half column of the last lane
         if (jh >= 0 && jh < N) bnd[jh] = Zout;
       }
     };
     int t = 0;
     for (; t + 1 < T_end; t += 2) {
-      // even step: profile words into WA, previous high words in WB
+      // even step: hi words into HA; the high half uses HB (previous column)
       int c = cnext;
       int jn = t + 1 + j0;
       cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodePad;
-      ST::load(tab, c, lane, WA);
+      ST::load_lo(tab, c, lane, Wlo);
+      ST::load_hi(tab, c, lane, HA);
       uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
-      ST::run(t, z, WA, WB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO);
+      ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale);
       out_bnd(t);
-      // odd step: into WB, previous high words in WA
+      // odd step: hi words into HB; the high half uses HA
       c = cnext;
       jn = t + 2 + j0;
       cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodePad;
-      ST::load(tab, c, lane, WB);
+      ST::load_lo(tab, c, lane, Wlo);
+      ST::load_hi(tab, c, lane, HB);
       z = top(t + 1, __shfl_up_sync(gmask, Zout, 1, G));
-      ST::run(t + 1, z, WB, WA, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO);
+      ST::run(t + 1, z, Wlo, HA, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale);
       out_bnd(t + 1);
     }
     if (t < T_end) {
-      ST::load(tab, cnext, lane, WA);
+      ST::load_lo(tab, cnext, lane, Wlo);
       const uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
-      ST::run(t, z, WA, WB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO);
+      ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale);
       out_bnd(t);
     }
 
@@ -207,8 +256,8 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
 #pragma unroll
     for (int half = 0; half < 2; half++) {
       const uint32_t key = half ? (Kl >> 16) : (Kl & 0xffffu);
-      const int v = (int)(key >> 3);
-      const int k = 7 - (int)(key & 7u);
+      const int v = (int)(key >> KB);
+      const int k = (int)KMASK - (int)(key & KMASK);
       const int r = row0 + (half ? K : 0) + k;
       const int jstep = (int)(half ? (Jp >> 16) : (Jp & 0xffffu));
       const int col = jstep - 2 * lane - half;

@@ -279,11 +279,21 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
       if (found || t >= M2) break;
       t = (2 * t < M2) ? 2 * t : M2;
     }
-    if (escalate) {
-      const int slot = atomicAdd(out_count, 1);
-      if (slot < cap) out_list[slot] = p;
-      continue;
+    // warp-aggregated append of the pairs that need a wider band
+    const unsigned act = __activemask();
+    const unsigned esc = __ballot_sync(act, escalate);
+    if (esc) {
+      const int leader = __ffs(esc) - 1;
+      const int lane32 = threadIdx.x & 31;
+      int base = 0;
+      if (lane32 == leader) base = atomicAdd(out_count, __popc(esc));
+      base = __shfl_sync(act, base, leader);
+      if (escalate) {
+        const int slot = base + __popc(esc & ((1u << lane32) - 1u));
+        if (slot < cap) out_list[slot] = p;
+      }
     }
+    if (escalate) continue;
     if (!found) {
       rs.flag[p] |= kFlagTooLong;  // inconsistent; reported as an error by the driver
       rs.a_beg[p] = -1;
@@ -425,8 +435,7 @@ __global__ void k_pack5(ResultSet rs, int64_t n, int32_t *out5) {
 __global__ void k_reset_lists(WorkLists wl) {
   *wl.ovf_count = 0;
   *wl.wide_count = 0;
-  *wl.esc1_count = 0;
-  *wl.esc2_count = 0;
+  for (int i = 0; i < kEscLevels; i++) wl.esc_counts[i] = 0;
 }
 
 int g_num_sms = 0;
@@ -440,16 +449,16 @@ int num_sms(int device) {
   return g_num_sms;
 }
 
-size_t group_prof16_rt(int K) {
-  switch (K) {
-    case 2: return group_prof16_bytes<2, kG>();
-    case 3: return group_prof16_bytes<3, kG>();
-    case 4: return group_prof16_bytes<4, kG>();
-    case 5: return group_prof16_bytes<5, kG>();
-    case 6: return group_prof16_bytes<6, kG>();
-    case 7: return group_prof16_bytes<7, kG>();
-    default: return group_prof16_bytes<8, kG>();
+size_t group_prof16_rt(int K, int G) {
+  if (G == kGKShort) {
+    switch (K) {
+      case 4: return group_prof16_bytes<4, kGKShort>();
+      case 6: return group_prof16_bytes<6, kGKShort>();
+      case 8: return group_prof16_bytes<8, kGKShort>();
+      default: return group_prof16_bytes<10, kGKShort>();
+    }
   }
+  return K == 6 ? group_prof16_bytes<6, kGKLong>() : group_prof16_bytes<8, kGKLong>();
 }
 
 size_t group_prof_rt(bool wide32, int K) {
@@ -480,15 +489,15 @@ cudaError_t launch_fwd_t(const FwdConfig &cfg, const PairSet &ps, const ResultSe
   return cudaGetLastError();
 }
 
-template <int K>
+template <int K, int G>
 cudaError_t launch_fwd16_t(const FwdConfig &cfg, const PairSet &ps, const ResultSet &rs, const Scoring &sc,
                            int ceiling, void *scratch, int scratch_stride, const WorkLists &wl, cudaStream_t st) {
-  auto kern = k_fwd16<K, kG>;
+  auto kern = k_fwd16<K, G>;
   if (cfg.smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
     if (e != cudaSuccess) return e;
   }
-  kern<<<cfg.grid, cfg.groups_per_block * kG, cfg.smem, st>>>(ps, rs, sc, ceiling,
+  kern<<<cfg.grid, cfg.groups_per_block * G, cfg.smem, st>>>(ps, rs, sc, ceiling,
                                                               reinterpret_cast<V16::Pay *>(scratch), scratch_stride,
                                                               wl, cfg.pad, cfg.bcap);
   return cudaGetLastError();
@@ -503,7 +512,10 @@ bool keyed_scoring(const Scoring &sc) {
 cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg, bool keyed) {
   FwdConfig c{};
   c.G = kG;
-  if (wide32) {
+  if (keyed && !wide32) {
+    c.G = keyed_g_for_rows(max_a);
+    c.K = keyed_k_for_rows(max_a);
+  } else if (wide32) {
     c.K = 4;
   } else {
     const int need = (max_a + 2 * kG - 1) / (2 * kG);  // K with 2*K*G >= max_a
@@ -515,16 +527,17 @@ cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfi
     else if (need <= 7) c.K = 7;
     else c.K = 8;
   }
-  c.pad = 2 * kG;
+  c.pad = 2 * c.G;
   if (max_b < 1) max_b = 1;
   if (max_b > kMaxB) return cudaErrorInvalidValue;
-  c.bcap = ((c.pad + max_b + 2 * kG) + 15) / 16 * 16;
+  c.bcap = ((c.pad + max_b + 2 * c.G) + 15) / 16 * 16;
   const size_t budget = 100 * 1024;  // keep two blocks per SM possible
   // the keyed engine reads B from global memory: its group needs the profile table only
   const size_t per_group =
-      (keyed && !wide32) ? group_prof16_rt(c.K) : group_prof_rt(wide32, c.K) + (size_t)c.bcap;
+      (keyed && !wide32) ? group_prof16_rt(c.K, c.G) : group_prof_rt(wide32, c.K) + (size_t)c.bcap;
   int gpb = 8;
   while (gpb > 1 && (size_t)gpb * per_group > budget) gpb /= 2;
+  if (c.G < kG) gpb *= kG / c.G;  // same block size (128 threads) with smaller groups
   c.groups_per_block = gpb;
   c.smem = (size_t)gpb * per_group;
   if (c.smem > 220 * 1024) return cudaErrorInvalidValue;
@@ -550,15 +563,16 @@ cudaError_t launch_forward(const FwdConfig &cfg, bool wide32, const PairSet &ps,
   const int stride = cfg.bcap;
   if (wide32) return launch_fwd_t<V32, 4>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
   if (cfg.keyed && !list) {
-    switch (cfg.K) {
-      case 2: return launch_fwd16_t<2>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
-      case 3: return launch_fwd16_t<3>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
-      case 4: return launch_fwd16_t<4>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
-      case 5: return launch_fwd16_t<5>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
-      case 6: return launch_fwd16_t<6>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
-      case 7: return launch_fwd16_t<7>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
-      default: return launch_fwd16_t<8>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+    if (cfg.G == kGKShort) {
+      switch (cfg.K) {
+        case 4: return launch_fwd16_t<4, kGKShort>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+        case 6: return launch_fwd16_t<6, kGKShort>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+        case 8: return launch_fwd16_t<8, kGKShort>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+        default: return launch_fwd16_t<10, kGKShort>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+      }
     }
+    if (cfg.K == 6) return launch_fwd16_t<6, kGKLong>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
+    return launch_fwd16_t<8, kGKLong>(cfg, ps, rs, sc, ceiling, scratch, stride, wl, st);
   }
   switch (cfg.K) {
     case 2: return launch_fwd_t<V16, 2>(cfg, ps, rs, sc, list, list_count, ceiling, scratch, stride, wl, st);
@@ -579,10 +593,22 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
     const int64_t blocks = (ps.n + 127) / 128;
     const int grid = (int)std::min<int64_t>(blocks, (int64_t)sms * 16);
     const int gridl = sms * 8;
-    k_rev_band<16><<<grid, 128, 0, st>>>(ps, rs, sc, order, nullptr, nullptr, wl.esc1, wl.esc1_count, wl.cap);
-    k_rev_band<32><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, wl.esc1, wl.esc1_count, wl.esc2, wl.esc2_count,
-                                          wl.cap);
-    k_rev_band<64><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, wl.esc2, wl.esc2_count, wl.wide, wl.wide_count,
+    // Band classes 7, 11, 15, 23, 31, 47, 63 cells; each kernel passes the pairs that need
+    // a wider band to the next one through alternating lists (esc1, esc2) with one
+    // counter per level (esc_counts[0..6]); the last level feeds wl.wide.
+    int64_t *lists[2] = {wl.esc1, wl.esc2};
+    k_rev_band<8><<<grid, 128, 0, st>>>(ps, rs, sc, order, nullptr, nullptr, lists[0], wl.esc_counts + 0, wl.cap);
+    k_rev_band<12><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[0], wl.esc_counts + 0, lists[1],
+                                          wl.esc_counts + 1, wl.cap);
+    k_rev_band<16><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[1], wl.esc_counts + 1, lists[0],
+                                          wl.esc_counts + 2, wl.cap);
+    k_rev_band<24><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[0], wl.esc_counts + 2, lists[1],
+                                          wl.esc_counts + 3, wl.cap);
+    k_rev_band<32><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[1], wl.esc_counts + 3, lists[0],
+                                          wl.esc_counts + 4, wl.cap);
+    k_rev_band<48><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[0], wl.esc_counts + 4, lists[1],
+                                          wl.esc_counts + 5, wl.cap);
+    k_rev_band<64><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[1], wl.esc_counts + 5, wl.wide, wl.wide_count,
                                           wl.cap);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;

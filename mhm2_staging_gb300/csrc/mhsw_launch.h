@@ -9,14 +9,16 @@ struct Scoring;
 struct PairSet;
 struct ResultSet;
 
+constexpr int kEscLevels = 8;
+
 // Work lists built on the device (no host round trip between passes).
 struct WorkLists {
   int64_t *ovf;       // pairs whose int16 forward pass crossed the ceiling
   int *ovf_count;
   int64_t *wide;      // pairs whose reverse band is wider than the banded kernels handle
   int *wide_count;
-  int64_t *esc1, *esc2;  // escalation lists between the banded begin kernels (16 -> 32 -> 64 cells)
-  int *esc1_count, *esc2_count;
+  int64_t *esc1, *esc2;  // alternating escalation lists between the banded begin kernels
+  int *esc_counts;       // kEscLevels counters, one per band level
   int64_t cap;        // capacity of each list
 };
 

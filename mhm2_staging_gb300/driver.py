@@ -109,6 +109,7 @@ SIGNATURES: dict[str, tuple] = {
     "mhsw_align_pairs": (C.c_int, [_P, C.POINTER(PairsT), _P, C.c_int, C.c_int]),
     "mhsw_last_timing": (C.c_int, [_P, C.POINTER(Timing)]),
     "mhsw_probe_dpx_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "mhsw_probe_op_rate": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }
 
 _LIB: C.CDLL | None = None
@@ -181,6 +182,14 @@ def probe_dpx_rate(device: int = 0) -> tuple[float, float]:
     ops, hz = C.c_double(0), C.c_double(0)
     _check(lib, lib.mhsw_probe_dpx_rate(device, C.byref(ops), C.byref(hz)), what="probe_dpx_rate")
     return ops.value, hz.value
+
+
+def probe_op_rate(op: int, device: int = 0) -> float:
+    """Lane operations per second of one instruction form (see include/mhsw.h)."""
+    lib = load_library()
+    v = C.c_double(0)
+    _check(lib, lib.mhsw_probe_op_rate(device, op, C.byref(v)), what="probe_op_rate")
+    return v.value
 
 
 def limits() -> Limits:
