@@ -1,4 +1,4 @@
-// adept_sw/driver.hpp -- header-only drop-in for the reference's GPU aligner class.
+// adept-sw/driver.hpp -- header-only drop-in for the reference's GPU aligner class.
 //
 // Same namespace, class and signatures as the reference header src/adept-sw/driver.hpp
 // (lines 14-57), implemented over the C ABI of include/mhsw.h (libmhsw.so).  A caller

@@ -85,7 +85,7 @@ def test_cpp_dropin_header_compiles_and_links(built, tmp_path):
 #include <cstdio>
 #include <string>
 #include <vector>
-#include "adept_sw/driver.hpp"
+#include "adept-sw/driver.hpp"
 int main() {
   int n = adept_sw::get_num_node_gpus();
   std::printf("gpus=%d\n", n);
