@@ -175,6 +175,33 @@ int mhsw_get_aln_results(mhsw_driver *drv, mhsw_aln_results *out);
 int mhsw_align_pairs(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form);
 int mhsw_last_timing(mhsw_driver *drv, mhsw_timing *out);
 
+/* ---- allocation-free forward pass (no counterpart in the reference) ---------- */
+/* Forward pass only -- score, a_end, b_end per pair, the same values as columns 0, 2
+ * and 4 of mhsw_align_pairs -- for callers that must not have the library allocate
+ * device memory: a process that has handed its device memory to its own pool up front,
+ * or a pipelined loop that cannot take the device-wide synchronisation cudaMalloc and
+ * cudaFree may imply.  Nothing in this call allocates (no cudaMalloc, cudaFree or
+ * allocating library routine); all scratch lives in one fixed 32 MiB device array inside
+ * the library, one per device.  No handle: the current device is used.
+ *   pairs : DEVICE pointers of a batch on the current device (raw bytes, any case, as
+ *           mhsw_align_pairs takes them); pairs->max_a_len and pairs->max_b_len are
+ *           required and must bound every pair (a pair beyond them gets -1, -1, -1).
+ *           Each lane group takes about 9 * max_b_len + max_a_len bytes of the scratch
+ *           array; a batch with max_b_len above 65000, max_a_len of 2^20 or more, or a
+ *           share beyond the whole array is rejected with MHSW_ERR_LIMIT.
+ *   scores: as mhsw_driver_init (match positive, penalties negated), plus ambiguity.
+ *   out3  : device array of 3 * n int32: score, a_end, b_end (score 0: 0, -1, 0).
+ *   stream: cudaStream_t to launch on (NULL: the default stream); returns without waiting.
+ *   errbuf: (may be NULL) receives a message when the call fails.
+ * The first call on a device does a one-time set-up with that device current (the
+ * scratch array's address, the kernel's attributes); make it before any stream capture.
+ * Calls race on the shared scratch array: two calls on one device must not overlap in
+ * time (issue them on one stream, or order them with events).  Nothing in the scratch
+ * array needs to start at zero. */
+int mhsw_forward_noalloc(const mhsw_pairs *pairs, short match_score, short mismatch_score, short gap_opening_score,
+                         short gap_extending_score, short ambiguity_score, int32_t *out3, void *stream, char *errbuf,
+                         size_t errlen);
+
 /* ---- diagnostics ----------------------------------------------------------- */
 /* Measures the device's packed int16 DPX add-max throughput (__viaddmax_s16x2 on
  * independent chains, all SMs busy): *ops_per_s = packed instructions per second over

@@ -108,6 +108,10 @@ SIGNATURES: dict[str, tuple] = {
     "mhsw_get_aln_results": (C.c_int, [_P, C.POINTER(_AlnResults)]),
     "mhsw_align_pairs": (C.c_int, [_P, C.POINTER(PairsT), _P, C.c_int, C.c_int]),
     "mhsw_last_timing": (C.c_int, [_P, C.POINTER(Timing)]),
+    "mhsw_forward_noalloc": (
+        C.c_int,
+        [C.POINTER(PairsT), C.c_short, C.c_short, C.c_short, C.c_short, C.c_short, _P, _P, C.c_char_p, C.c_size_t],
+    ),
     "mhsw_probe_dpx_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "mhsw_probe_op_rate": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }
@@ -197,6 +201,19 @@ def limits() -> Limits:
     out = Limits()
     lib.mhsw_limits(C.byref(out))
     return out
+
+
+def forward_noalloc(dev: "DevicePairs", out3_dev_ptr: int, scores=(1, -3, -5, -2, -2), stream: int = 0) -> None:
+    """Forward pass (score, a_end, b_end per pair into the device buffer out3_dev_ptr,
+    n x 3 int32) through mhsw_forward_noalloc, which allocates no device memory; dev
+    must carry max_a_len and max_b_len.  scores = (match, mismatch, gap open, gap extend,
+    ambiguity), penalties negated.  Asynchronous on `stream` (a cudaStream_t value)."""
+    lib = load_library()
+    pt = dev.c_struct()
+    err = C.create_string_buffer(256)
+    rc = lib.mhsw_forward_noalloc(C.byref(pt), *scores, _P(out3_dev_ptr), _P(stream or None), err, len(err))
+    if rc != 0:
+        raise RuntimeError(f"forward_noalloc failed (status {rc}): {err.value.decode()}")
 
 
 @dataclass
