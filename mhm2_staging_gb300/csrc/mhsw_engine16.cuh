@@ -11,8 +11,10 @@
 //     multiply-adds (FMA pipe) from two table words, one per half, each already
 //     biased by +gO; this needs s + gO >= 0 for every score (mismatch and ambiguity
 //     not above the gap-open penalty), which the driver checks before choosing this
-//     engine.  PAD cells score -gO (biased 0), which keeps every value outside the
-//     matrix below the pair's maximum.
+//     engine.  Rows past the end of A score -gO (biased 0); columns outside B read as
+//     N (score -ambiguity <= 0).  Cells left of column 0 then stay exactly 0, and every
+//     cell right of the last column is at most a real cell of a smaller row, so no
+//     value outside the matrix can win the arg-max or raise a false overflow.
 //  2. The arg-max is tracked per lane half, not per row: each cell contributes the
 //     16-bit key H*2^b + (2^b-1-k) (k = row within the half, b = 3 for up to 8 rows
 //     per half, else 4), so the maximum key is the
@@ -21,9 +23,12 @@
 //     first column at which that row reached that score -- the lexicographic rule of
 //     SSW (ssw_core.cpp:474-506).  Keys need H < 2^(15-b), so this engine flags pairs
 //     whose score reaches the ceiling (at most KeyBits::kCap) for the int32 engine.
-//  3. The profile table holds separate low-half and high-half words, loaded as 128-bit
-//     vectors; the high words loaded at step t serve the high half at step t+1 (the
-//     step loop is unrolled by two so the two word sets alternate registers).
+//  3. The profile table holds separate low-half and high-half words for the five B
+//     codes, loaded as 128-bit vectors: K/4 vectors of low words, K/4 of high words and,
+//     when K is 2 mod 4, one vector holding the last two low and the last two high
+//     words (every load is a full 128-bit vector, conflict-free across the groups of a
+//     warp).  The high words loaded at step t serve the high half at step t+1 (the step
+//     loop is unrolled by two so the two word sets alternate registers).
 //  4. B codes are read from global memory (prefetched a step ahead) instead of being
 //     staged in shared memory, so a group's shared memory is its profile table only.
 #pragma once
@@ -45,10 +50,17 @@ __host__ __device__ constexpr int keyed_cap(int K) { return K <= 8 ? (1 << 12) -
 
 template <int K>
 struct Prof16 {
-  static constexpr int kNQh = (K + 3) / 4;   // 128-bit vectors per half (lo words, then hi words)
-  static constexpr int kNQ = 2 * kNQh;
-  static constexpr int kWh = 4 * kNQh;       // words per half, padded
-  __host__ __device__ static constexpr size_t bytes(int lanes) { return (size_t)kNumCodes * kNQ * lanes * 16; }
+  static_assert(K % 2 == 0, "row pairs per lane must be even");
+  static constexpr int kCodes = kCodeN + 1;   // B codes A, C, G, T, N (outside B reads as N)
+  static constexpr int kQ = K / 4;            // full vectors of low words (and of high words)
+  static constexpr bool kRem = (K % 4) != 0;  // one vector: low K-2, K-1, high K-2, K-1
+  static constexpr int kNV = 2 * kQ + (kRem ? 1 : 0);  // 128-bit vectors per (code, lane)
+  __host__ __device__ static constexpr size_t bytes(int lanes) { return (size_t)kCodes * kNV * lanes * 16; }
+  // vector and element of low word w / high word w
+  __host__ __device__ static constexpr int lo_vec(int w) { return w < 4 * kQ ? w / 4 : 2 * kQ; }
+  __host__ __device__ static constexpr int lo_elem(int w) { return w < 4 * kQ ? w % 4 : w - 4 * kQ; }
+  __host__ __device__ static constexpr int hi_vec(int w) { return w < 4 * kQ ? kQ + w / 4 : 2 * kQ; }
+  __host__ __device__ static constexpr int hi_elem(int w) { return w < 4 * kQ ? w % 4 : 2 + w - 4 * kQ; }
 };
 
 template <int KMAX, int G>
@@ -84,8 +96,8 @@ template <int K, int G>
 struct Step16 {
   using L = Prof16<K>;
   static constexpr uint32_t kKeyMask = KeyBits<K>::kMask;
-  __device__ static __forceinline__ void run(int t, uint32_t z, const uint32_t (&Wlo)[L::kWh],
-                                             const uint32_t (&Phi)[L::kWh], uint32_t (&H)[K], uint32_t (&F)[K],
+  __device__ static __forceinline__ void run(int t, uint32_t z, const uint32_t (&Wlo)[K],
+                                             const uint32_t (&Phi)[K], uint32_t (&H)[K], uint32_t (&F)[K],
                                              uint32_t &Hlast, uint32_t &Ecout, uint32_t &HtopPrev, uint32_t &Zout,
                                              uint32_t &Kl, uint32_t &Jp, uint32_t NGE, uint32_t NGO, uint32_t one,
                                              uint32_t eight) {
@@ -107,40 +119,43 @@ struct Step16 {
       H[k] = Hn;
       key[k] = mad_u32(Hn, eight, (uint32_t)(kKeyMask - k) * 0x00010001u);
     }
-    uint32_t km = key[0];
+    // running key per half (keys are non-negative int16): K/2 three-way maxima
+    uint32_t Kn = Kl;
 #pragma unroll
-    for (int k = 1; k + 1 < K; k += 2) km = __vimax3_s16x2(km, key[k], key[k + 1]);
-    if ((K % 2) == 0) km = __vimax_s16x2_relu(km, key[K - 1]);
+    for (int k = 0; k < K; k += 2) Kn = __vimax3_s16x2(Kn, key[k], key[k + 1]);
     Zout = __byte_perm(H[K - 1], Ev, 0x7632);
     Hlast = H[K - 1];
     Ecout = Ev;
-    // running key per half; record the step where it strictly grows
-    const uint32_t Kn = __vimax_s16x2_relu(Kl, km);
+    // record the step where the running key strictly grows
     const uint32_t msk = sign_mask16(Kn - Kl + 0x7fff7fffu);
     const uint32_t tt = (uint32_t)t * 0x00010001u;
     Jp = (msk & tt) | (~msk & Jp);
     Kl = Kn;
   }
-  // lo words of code c (used at this step)
-  __device__ static __forceinline__ void load_lo(const uint4 *tab, int c, int lane, uint32_t (&W)[L::kWh]) {
+  // Words of code c: low words into Wlo (used at this step), high words into Whi (used
+  // at the next step by the high half).
+  __device__ static __forceinline__ void load(const uint4 *tab, int c, int lane, uint32_t (&Wlo)[K],
+                                              uint32_t (&Whi)[K]) {
+    const uint4 *b = tab + c * L::kNV * G + lane;
 #pragma unroll
-    for (int q = 0; q < L::kNQh; q++) {
-      const uint4 v = tab[(c * L::kNQ + q) * G + lane];
-      W[4 * q + 0] = v.x;
-      W[4 * q + 1] = v.y;
-      W[4 * q + 2] = v.z;
-      W[4 * q + 3] = v.w;
+    for (int q = 0; q < L::kQ; q++) {
+      const uint4 v = b[q * G];
+      Wlo[4 * q + 0] = v.x;
+      Wlo[4 * q + 1] = v.y;
+      Wlo[4 * q + 2] = v.z;
+      Wlo[4 * q + 3] = v.w;
+      const uint4 u = b[(L::kQ + q) * G];
+      Whi[4 * q + 0] = u.x;
+      Whi[4 * q + 1] = u.y;
+      Whi[4 * q + 2] = u.z;
+      Whi[4 * q + 3] = u.w;
     }
-  }
-  // hi words of code c (used at the next step by the high half)
-  __device__ static __forceinline__ void load_hi(const uint4 *tab, int c, int lane, uint32_t (&W)[L::kWh]) {
-#pragma unroll
-    for (int q = 0; q < L::kNQh; q++) {
-      const uint4 v = tab[(c * L::kNQ + L::kNQh + q) * G + lane];
-      W[4 * q + 0] = v.x;
-      W[4 * q + 1] = v.y;
-      W[4 * q + 2] = v.z;
-      W[4 * q + 3] = v.w;
+    if constexpr (L::kRem) {
+      const uint4 v = b[2 * L::kQ * G];
+      Wlo[K - 2] = v.x;
+      Wlo[K - 1] = v.y;
+      Whi[K - 2] = v.z;
+      Whi[K - 1] = v.w;
     }
   }
 };
@@ -178,30 +193,28 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
     // Profile words: lo word k = s(A[row0+k], c) + gO; hi word k = (s(A[row0+K+k], c) + gO) << 16.
     {
       uint32_t *tw = gs.prof;
-      for (int c = 0; c < kNumCodes; c++) {
+      for (int c = 0; c < L::kCodes; c++) {
 #pragma unroll
-        for (int w = 0; w < L::kWh; w++) {
-          const uint32_t vlo =
-              w < K ? (uint32_t)(sub_score(A.code(row0 + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu : 0u;
-          const uint32_t vhi =
-              w < K ? ((uint32_t)(sub_score(A.code(row0 + K + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu) << 16
-                    : 0u;
-          const int q = w / 4, r = w % 4;
-          tw[((c * L::kNQ + q) * G + lane) * 4 + r] = vlo;
-          tw[((c * L::kNQ + L::kNQh + q) * G + lane) * 4 + r] = vhi;
+        for (int w = 0; w < K; w++) {
+          const uint32_t vlo = (uint32_t)(sub_score(A.code(row0 + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu;
+          const uint32_t vhi = ((uint32_t)(sub_score(A.code(row0 + K + w), c, sc, sc.gap_open) + sc.gap_open) &
+                                0xffffu)
+                               << 16;
+          tw[((c * L::kNV + L::lo_vec(w)) * G + lane) * 4 + L::lo_elem(w)] = vlo;
+          tw[((c * L::kNV + L::hi_vec(w)) * G + lane) * 4 + L::hi_elem(w)] = vhi;
         }
       }
     }
     __syncwarp(gmask);
 
-    uint32_t H[K], F[K], Wlo[L::kWh], HA[L::kWh], HB[L::kWh];
+    uint32_t H[K], F[K], Wlo[K], HA[K], HB[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
       H[k] = 0u;
       F[k] = 0u;  // F^ = F + gO with F = -gO before column 0
     }
 #pragma unroll
-    for (int w = 0; w < L::kWh; w++) HB[w] = 0u;  // hi words of the PAD column before column 0 (biased 0)
+    for (int w = 0; w < K; w++) HB[w] = 0u;  // hi words before column 0 (biased 0)
     uint32_t Hlast = 0u, Ecout = 0u, HtopPrev = 0u;
     uint32_t Zout = 0u;  // (lo: H of the hi-last row, hi: E^ below it)
     uint32_t Kl = 0u;    // running key per half
@@ -209,7 +222,7 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
     const bool first_strip = (s == 0);
     const bool last_strip = (s == nstrips - 1);
     const int j0 = -2 * lane;  // lo column at step 0
-    int cnext = (j0 >= 0 && j0 < N) ? (int)bg[j0] : kCodePad;
+    int cnext = (j0 >= 0 && j0 < N) ? (int)bg[j0] : kCodeN;
 
     auto top = [&](int t, uint32_t zs) -> uint32_t {
       uint32_t z = zs & zmask;
@@ -227,24 +240,22 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
       // even step: hi words into HA; the high half uses HB (previous column)
       int c = cnext;
       int jn = t + 1 + j0;
-      cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodePad;
-      ST::load_lo(tab, c, lane, Wlo);
-      ST::load_hi(tab, c, lane, HA);
+      cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodeN;
+      ST::load(tab, c, lane, Wlo, HA);
       uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
       ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale);
       out_bnd(t);
       // odd step: hi words into HB; the high half uses HA
       c = cnext;
       jn = t + 2 + j0;
-      cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodePad;
-      ST::load_lo(tab, c, lane, Wlo);
-      ST::load_hi(tab, c, lane, HB);
+      cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodeN;
+      ST::load(tab, c, lane, Wlo, HB);
       z = top(t + 1, __shfl_up_sync(gmask, Zout, 1, G));
       ST::run(t + 1, z, Wlo, HA, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale);
       out_bnd(t + 1);
     }
     if (t < T_end) {
-      ST::load_lo(tab, cnext, lane, Wlo);
+      ST::load(tab, cnext, lane, Wlo, HA);
       const uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
       ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale);
       out_bnd(t);
