@@ -39,6 +39,7 @@ extern "C" {
 #define MHSW_ERR_LIMIT 5     /* a sequence exceeds the engine limits (see mhsw_limits) */
 #define MHSW_ERR_NO_GPU 6    /* no CUDA device */
 #define MHSW_ERR_INTERNAL 7  /* internal consistency check failed */
+#define MHSW_ERR_BUSY 8      /* serving queue full (submit with MHSW_SUBMIT_NOWAIT) */
 
 /* ---- orientation ----------------------------------------------------------- */
 /* klign (default): reads are SSW's ref (A), contigs its query (B); results map
@@ -174,6 +175,74 @@ int mhsw_get_aln_results(mhsw_driver *drv, mhsw_aln_results *out);
  * SSW query = B; score 0 gives -1, -1, 0, 0 as SSW does). */
 int mhsw_align_pairs(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form);
 int mhsw_last_timing(mhsw_driver *drv, mhsw_timing *out);
+
+/* ---- serving form (no counterpart in the reference) ------------------------ */
+/* Contigs stay resident on the device (translated once); alignment requests -- a read
+ * plus the contig and position its k-mer seed hit points to -- arrive in uneven batches
+ * from any number of host threads.  Each request's pair is the read against the contig
+ * window [max(0, pos - flank), min(contig_len, pos + read_len + flank)), the window klign
+ * cuts around a seed hit (src/klign.cpp:670-739).  Worker slots, each with its own stream
+ * and device buffers sized from the device-memory budget, pack whatever requests are
+ * waiting into the next micro-batch as soon as they free up (continuous batching), so
+ * requests that arrive while others are on the GPU join the next free slot and the slots'
+ * work overlaps on the device.  Results are those of mhsw_align_pairs on the same pairs,
+ * whatever else shares the micro-batch. */
+typedef struct mhsw_server mhsw_server;
+
+typedef struct {
+  int device;                   /* CUDA device */
+  int slots;                    /* micro-batches in flight at once (0: 3) */
+  int32_t max_pairs_per_batch;  /* pairs per micro-batch (0: 65536) */
+  int32_t flank;                /* window flank in bases (negative: 200) */
+  size_t hbm_budget;            /* device bytes for contigs plus slots (0: half the free memory) */
+  size_t queue_budget;          /* host bytes of admitted requests not yet finished (0: 1 GiB) */
+  short match_score, mismatch_score, gap_opening_score, gap_extending_score, ambiguity_score; /* as klign passes them */
+  int form;                     /* MHSW_FORM_BATCHED or MHSW_FORM_PLAIN */
+} mhsw_server_config;
+
+typedef struct {   /* host pointers; copied by mhsw_server_submit */
+  const char *read_seq;
+  const int64_t *read_off;
+  const int32_t *read_len;
+  const int32_t *contig_id;   /* index into the loaded contigs */
+  const int32_t *contig_pos;  /* seed-hit position in the contig, 0 <= pos < contig_len */
+  int32_t n;
+} mhsw_requests;
+
+typedef struct {
+  int64_t submitted, completed;   /* request batches */
+  int64_t pairs_done;
+  double cells_done;              /* sum of read_len * window_len over finished pairs */
+  int64_t micro_batches;
+  int64_t queued_pairs;           /* admitted, not yet on a slot */
+  size_t admitted_bytes;          /* host bytes of admitted, unfinished requests */
+  int slots, busy_slots;
+  int32_t slot_pairs;             /* pairs per micro-batch */
+  size_t device_bytes;            /* contig store + slot buffers */
+} mhsw_server_stats;
+
+#define MHSW_SUBMIT_NOWAIT 1       /* fail with MHSW_ERR_BUSY instead of waiting for queue room */
+
+/* Creates a server (no device memory yet).  errbuf (may be NULL) receives a message. */
+int mhsw_server_create(const mhsw_server_config *cfg, mhsw_server **out, char *errbuf, size_t errlen);
+/* Stops the slots after their current micro-batch; unfinished requests fail. */
+void mhsw_server_destroy(mhsw_server *s);
+const char *mhsw_server_last_error(const mhsw_server *s);
+/* Uploads and translates the contigs (host pointers), then sizes and starts the slots
+ * from what is left of the budget.  Once per server. */
+int mhsw_server_load_contigs(mhsw_server *s, const char *seq, const int64_t *off, const int32_t *len, int64_t count);
+/* Admits a request batch (copied) once the queue budget has room; results go to out5
+ * (5 * n int32: score, a_begin, a_end, b_begin, b_end, B coordinates relative to the
+ * window) and win_start (n int64, may be NULL: contig offset of each window) when the
+ * ticket completes; both must stay valid until mhsw_server_wait returns. */
+int mhsw_server_submit(mhsw_server *s, const mhsw_requests *req, int32_t *out5, int64_t *win_start, int flags,
+                       uint64_t *ticket);
+/* *done = 1 once the ticket's results are written. */
+int mhsw_server_test(mhsw_server *s, uint64_t ticket, int *done);
+/* Waits for the ticket, returns its status and releases it.  times (may be NULL)
+ * receives submit, first dispatch and completion times in seconds (steady clock). */
+int mhsw_server_wait(mhsw_server *s, uint64_t ticket, double *times3);
+int mhsw_server_stats_get(mhsw_server *s, mhsw_server_stats *out);
 
 /* ---- allocation-free forward pass (no counterpart in the reference) ---------- */
 /* Forward pass only -- score, a_end, b_end per pair, the same values as columns 0, 2

@@ -236,4 +236,128 @@ const int32_t *mhsw_gen_read_len(void *h) { return ((PairSet *)h)->rlen.data(); 
 const int32_t *mhsw_gen_ref_len(void *h) { return ((PairSet *)h)->flen.data(); }
 void mhsw_gen_free(void *h) { delete (PairSet *)h; }
 
+// ---- config 3 (serving): a resident contig set and requests against it ------------------
+
+struct ContigSet {
+  std::string seq;
+  std::vector<int64_t> off;  // count + 1
+  std::vector<int32_t> len;
+};
+
+// Contigs with lengths round(lognormal(ln 2000, 1.0)) clamped to [200, 200000], drawn from
+// one stream until the total reaches total_bytes; the bases of contig c come from stream
+// splitmix64(seed, c + 1) (uniform ACGT).
+void *mhsw_gen_contigs(uint64_t seed, int64_t total_bytes, int nthreads) {
+  ContigSet *cs = new ContigSet();
+  Rng r(splitmix64(seed * 0x100000001B3ull));
+  int64_t tot = 0;
+  while (tot < total_bytes) {
+    double ln = std::log(2000.0) + 1.0 * r.normal();
+    int64_t L = (int64_t)std::llround(std::exp(ln));
+    L = std::min<int64_t>(std::max<int64_t>(L, 200), 200000);
+    cs->off.push_back(tot);
+    cs->len.push_back((int32_t)L);
+    tot += L;
+  }
+  cs->off.push_back(tot);
+  cs->seq.resize((size_t)tot);
+  const int64_t nc = (int64_t)cs->len.size();
+  if (nthreads < 1) nthreads = 1;
+  auto work = [&](int tid) {
+    for (int64_t c = tid; c < nc; c += nthreads) {
+      Rng g(splitmix64(seed * 0x100000001B3ull + (uint64_t)c + 1));
+      char *dst = &cs->seq[(size_t)cs->off[(size_t)c]];
+      for (int32_t k = 0; k < cs->len[(size_t)c]; k++) dst[k] = g.base();
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nthreads; t++) th.emplace_back(work, t);
+  work(0);
+  for (auto &t : th) t.join();
+  return cs;
+}
+
+int64_t mhsw_gen_contig_count(void *h) { return (int64_t)((ContigSet *)h)->len.size(); }
+const char *mhsw_gen_contig_seq(void *h) { return ((ContigSet *)h)->seq.data(); }
+const int64_t *mhsw_gen_contig_off(void *h) { return ((ContigSet *)h)->off.data(); }
+const int32_t *mhsw_gen_contig_len(void *h) { return ((ContigSet *)h)->len.data(); }
+void mhsw_gen_contigs_free(void *h) { delete (ContigSet *)h; }
+
+struct RequestSet {
+  std::string reads;
+  std::vector<int64_t> off;  // count + 1
+  std::vector<int32_t> len, cid, pos;
+};
+
+// Requests [first, first + count) against a contig set (bytes, offsets, lengths, as
+// host arrays): request q draws from stream
+// splitmix64(seed, q / 1024).  L ~ U[100, 250]; a uniform base over the whole set picks
+// the contig (length-weighted) and the seed-hit position pos, moved left so the read fits
+// when it can; the read is contig[pos, pos + L) (clipped at the contig end) with 1.5%
+// substitutions and 0.5% 1-bp indels (2% divergence).
+void *mhsw_gen_requests(const char *cseq, const int64_t *coff, const int32_t *clen, int64_t ncontigs, uint64_t seed,
+                        int64_t first, int64_t count, int nthreads) {
+  const int64_t kChunk = 1024;
+  RequestSet *rs = new RequestSet();
+  rs->off.push_back(0);
+  if (count <= 0 || ncontigs <= 0) return rs;
+  std::vector<int64_t> cum((size_t)ncontigs + 1, 0);  // length-weighted choice of the contig
+  for (int64_t c = 0; c < ncontigs; c++) cum[(size_t)c + 1] = cum[(size_t)c] + clen[c];
+  const int64_t total = cum.back();
+  if (total <= 0) return rs;
+  int64_t c0 = first / kChunk, c1 = (first + count - 1) / kChunk;
+  int64_t nchunks = c1 - c0 + 1;
+  struct RChunk {
+    std::string reads;
+    std::vector<int32_t> len, cid, pos;
+  };
+  std::vector<RChunk> chunks((size_t)nchunks);
+  if (nthreads < 1) nthreads = 1;
+  auto work = [&](int tid) {
+    std::string src, read;
+    for (int64_t ci = tid; ci < nchunks; ci += nthreads) {
+      const int64_t c = c0 + ci;
+      Rng r(splitmix64((seed + 0x5151) * 0x100000001B3ull + (uint64_t)c));
+      RChunk &ch = chunks[(size_t)ci];
+      for (int64_t k = 0; k < kChunk; k++) {
+        const int64_t q = c * kChunk + k;
+        const int64_t L = r.uint_in(100, 250);
+        const int64_t u = r.uint_in(0, total - 1);
+        const int64_t id = (int64_t)(std::upper_bound(cum.begin(), cum.end(), u) - cum.begin()) - 1;
+        const int64_t cl = clen[id];
+        int64_t pos = u - cum[(size_t)id];
+        pos = std::min<int64_t>(pos, std::max<int64_t>(0, cl - L));
+        const int64_t take = std::min<int64_t>(L, cl - pos);
+        src.assign(cseq + coff[id] + pos, (size_t)take);
+        mutate(r, src, 0.015, 0.005, read);
+        if (q < first || q >= first + count) continue;
+        ch.reads += read;
+        ch.len.push_back((int32_t)read.size());
+        ch.cid.push_back((int32_t)id);
+        ch.pos.push_back((int32_t)pos);
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nthreads; t++) th.emplace_back(work, t);
+  work(0);
+  for (auto &t : th) t.join();
+  for (auto &ch : chunks) {
+    for (size_t k = 0; k < ch.len.size(); k++) rs->off.push_back(rs->off.back() + ch.len[k]);
+    rs->reads += ch.reads;
+    rs->len.insert(rs->len.end(), ch.len.begin(), ch.len.end());
+    rs->cid.insert(rs->cid.end(), ch.cid.begin(), ch.cid.end());
+    rs->pos.insert(rs->pos.end(), ch.pos.begin(), ch.pos.end());
+  }
+  return rs;
+}
+
+int64_t mhsw_gen_request_count(void *h) { return (int64_t)((RequestSet *)h)->len.size(); }
+const char *mhsw_gen_request_reads(void *h) { return ((RequestSet *)h)->reads.data(); }
+const int64_t *mhsw_gen_request_off(void *h) { return ((RequestSet *)h)->off.data(); }
+const int32_t *mhsw_gen_request_len(void *h) { return ((RequestSet *)h)->len.data(); }
+const int32_t *mhsw_gen_request_cid(void *h) { return ((RequestSet *)h)->cid.data(); }
+const int32_t *mhsw_gen_request_pos(void *h) { return ((RequestSet *)h)->pos.data(); }
+void mhsw_gen_requests_free(void *h) { delete (RequestSet *)h; }
+
 }  // extern "C"

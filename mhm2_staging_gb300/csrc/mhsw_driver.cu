@@ -20,6 +20,7 @@
 #include "mhsw_batch.h"
 #include "mhsw_engine.cuh"
 #include "mhsw_engine16.cuh"
+#include "mhsw_internal.h"
 #include "mhsw_launch.h"
 
 namespace {
@@ -121,6 +122,9 @@ struct mhsw_driver {
   bool rev_issued = false;
   double fwd_cells = 0;
   int64_t launches = 0;
+  // Pair order of the last forward pass when it ran the batched form (its sorted
+  // order, reused by the begin pass for coherent warps); null after a plain pass.
+  const uint32_t *fwd_order = nullptr;
   mhsw_timing timing{};
 
   int fail(int code, const char *fmt, ...) {
@@ -296,6 +300,7 @@ int run_forward(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, b
 int forward_any(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, int form) {
   // The batched form runs the keyed int16 engine; scorings it cannot hold (a mismatch or
   // ambiguity penalty above the gap-open penalty) use the plain form.
+  d->fwd_order = nullptr;
   if (form != MHSW_FORM_BATCHED || !mhsw::keyed_scoring(d->sc)) return run_forward(d, ps, max_a, max_b, false);
   mhsw::WorkLists wl = work_lists(d, ps.n);
   MHSW_CK(mhsw::reset_lists(wl, d->st), "reset lists");
@@ -303,6 +308,7 @@ int forward_any(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, i
   if (mhsw::batched_forward(d->batch, d->device, ps, result_set(d), wl, d->sc, ceiling_for(d), max_a, max_b, d->st,
                             &d->launches))
     return d->fail(MHSW_ERR_CUDA, "batched forward: %s", d->batch.err.c_str());
+  d->fwd_order = d->batch.idx_out;
   // int32 pass over the pairs the int16 engine could not hold
   mhsw::FwdConfig c16, c32;
   if (mhsw::plan_forward(d->device, max_a, max_b, false, &c16) != cudaSuccess ||
@@ -683,7 +689,7 @@ int mhsw_run_kernel_backwards(mhsw_driver *d, const char *const *reads, const in
   mhsw::PairSet ps = staged_pairs(d);
   MHSW_CK(cudaEventRecord(d->ev_t[4], d->st), "event");
   if (n > 0) {
-    rc = run_reverse(d, ps, d->max_a, d->max_b, d->form == MHSW_FORM_BATCHED ? d->batch.idx_out : nullptr);
+    rc = run_reverse(d, ps, d->max_a, d->max_b, d->fwd_order);
     if (rc) return rc;
   }
   mhsw::OutViews dv, hv;
@@ -869,7 +875,7 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
   }
   MHSW_CK(cudaEventRecord(d->ev_t[2], d->st), "event");
   if (n > 0) {
-    rc = run_reverse(d, ps, ma, mb, form == MHSW_FORM_BATCHED ? d->batch.idx_out : nullptr);
+    rc = run_reverse(d, ps, ma, mb, d->fwd_order);
     if (rc) return rc;
   }
   MHSW_CK(cudaEventRecord(d->ev_t[3], d->st), "event");
@@ -908,3 +914,40 @@ int mhsw_last_timing(mhsw_driver *d, mhsw_timing *out) {
 }
 
 }  // extern "C"
+
+namespace mhsw {
+
+int align_resident(mhsw_driver *d, const PairSet &in, int64_t a_bytes, int max_a, int max_b, int form,
+                   int32_t *out5_dev) {
+  int rc = ready(d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (form != MHSW_FORM_PLAIN && form != MHSW_FORM_BATCHED) return d->fail(MHSW_ERR_ARG, "unknown form %d", form);
+  if (d->ev_live) MHSW_CK(cudaEventSynchronize(d->ev_done), "wait previous batch");
+  d->ev_live = false;
+  d->fwd_issued = d->rev_issued = false;
+  d->launches = 0;
+  const int64_t n = in.n;
+  if (n <= 0) return MHSW_OK;
+  if (!in.b_code || !out5_dev) return d->fail(MHSW_ERR_ARG, "resident batch needs B codes and an output buffer");
+  if (max_b > kMaxB) return d->fail(MHSW_ERR_LIMIT, "sequence of %d bytes exceeds the limit %d", max_b, kMaxB);
+  rc = ensure_results(d, n);
+  if (rc) return rc;
+  MHSW_CK(d->a_code.reserve((size_t)a_bytes + 16), "cudaMalloc codes");
+  MHSW_CK(launch_translate(in.a_seq, d->a_code.p, a_bytes, d->st), "translate A");
+  d->launches += 1;
+  PairSet ps = in;
+  ps.a_code = d->a_code.p;
+  rc = forward_any(d, ps, max_a, max_b, form);
+  if (rc) return rc;
+  rc = run_reverse(d, ps, max_a, max_b, d->fwd_order);
+  if (rc) return rc;
+  MHSW_CK(launch_pack5(result_set(d), n, out5_dev, d->st), "pack5");
+  d->launches += 1;
+  return MHSW_OK;
+}
+
+void *driver_stream(mhsw_driver *d) { return d ? static_cast<void *>(d->st) : nullptr; }
+int driver_device(mhsw_driver *d) { return d ? d->device : -1; }
+
+}  // namespace mhsw

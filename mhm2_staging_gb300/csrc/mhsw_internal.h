@@ -1,0 +1,24 @@
+// mhsw_internal.h -- entry points shared between the library's own translation units
+// (not part of the C ABI).
+#pragma once
+#include <cstdint>
+
+#include "../../include/mhsw.h"
+#include "mhsw_types.h"
+
+namespace mhsw {
+
+// Aligns a device-resident batch on a driver handle whose A side is raw bytes
+// (ps.a_seq, translated here into the handle's code buffer) and whose B side is an
+// already translated code arena that stays resident across calls (ps.b_code; ps.b_seq
+// is not read).  Forward and begin passes run on the handle's stream; out5_dev (device,
+// 5 int32 per pair: score, a_begin, a_end, b_begin, b_end) is written by the last
+// kernel.  Returns without waiting: the caller synchronises the handle's stream.
+int align_resident(mhsw_driver *d, const PairSet &ps, int64_t a_bytes, int max_a, int max_b, int form,
+                   int32_t *out5_dev);
+
+// The handle's stream (cudaStream_t) and device.
+void *driver_stream(mhsw_driver *d);
+int driver_device(mhsw_driver *d);
+
+}  // namespace mhsw

@@ -81,6 +81,53 @@ class PairsT(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [
+        ("device", C.c_int),
+        ("slots", C.c_int),
+        ("max_pairs_per_batch", C.c_int32),
+        ("flank", C.c_int32),
+        ("hbm_budget", C.c_size_t),
+        ("queue_budget", C.c_size_t),
+        ("match_score", C.c_short),
+        ("mismatch_score", C.c_short),
+        ("gap_opening_score", C.c_short),
+        ("gap_extending_score", C.c_short),
+        ("ambiguity_score", C.c_short),
+        ("form", C.c_int),
+    ]
+
+
+class RequestsT(C.Structure):
+    _fields_ = [
+        ("read_seq", _P),
+        ("read_off", _P),
+        ("read_len", _P),
+        ("contig_id", _P),
+        ("contig_pos", _P),
+        ("n", C.c_int32),
+    ]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [
+        ("submitted", C.c_int64),
+        ("completed", C.c_int64),
+        ("pairs_done", C.c_int64),
+        ("cells_done", C.c_double),
+        ("micro_batches", C.c_int64),
+        ("queued_pairs", C.c_int64),
+        ("admitted_bytes", C.c_size_t),
+        ("slots", C.c_int),
+        ("busy_slots", C.c_int),
+        ("slot_pairs", C.c_int32),
+        ("device_bytes", C.c_size_t),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # Every symbol include/mhsw.h declares, with its ctypes signature.
 SIGNATURES: dict[str, tuple] = {
     "mhsw_get_num_node_gpus": (C.c_int, [C.POINTER(C.c_int)]),
@@ -108,6 +155,14 @@ SIGNATURES: dict[str, tuple] = {
     "mhsw_get_aln_results": (C.c_int, [_P, C.POINTER(_AlnResults)]),
     "mhsw_align_pairs": (C.c_int, [_P, C.POINTER(PairsT), _P, C.c_int, C.c_int]),
     "mhsw_last_timing": (C.c_int, [_P, C.POINTER(Timing)]),
+    "mhsw_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P), C.c_char_p, C.c_size_t]),
+    "mhsw_server_destroy": (None, [_P]),
+    "mhsw_server_last_error": (C.c_char_p, [_P]),
+    "mhsw_server_load_contigs": (C.c_int, [_P, _P, _P, _P, C.c_int64]),
+    "mhsw_server_submit": (C.c_int, [_P, C.POINTER(RequestsT), _P, _P, C.c_int, C.POINTER(C.c_uint64)]),
+    "mhsw_server_test": (C.c_int, [_P, C.c_uint64, C.POINTER(C.c_int)]),
+    "mhsw_server_wait": (C.c_int, [_P, C.c_uint64, C.POINTER(C.c_double)]),
+    "mhsw_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
     "mhsw_forward_noalloc": (
         C.c_int,
         [C.POINTER(PairsT), C.c_short, C.c_short, C.c_short, C.c_short, C.c_short, _P, _P, C.c_char_p, C.c_size_t],
