@@ -200,7 +200,8 @@ typedef struct {
   int form;                     /* MHSW_FORM_BATCHED or MHSW_FORM_PLAIN */
 } mhsw_server_config;
 
-typedef struct {   /* host pointers; copied by mhsw_server_submit */
+typedef struct {   /* host pointers; offsets, lengths, ids and positions are copied by
+                    * mhsw_server_submit, the read bytes are read until the ticket completes */
   const char *read_seq;
   const int64_t *read_off;
   const int32_t *read_len;
@@ -231,10 +232,10 @@ const char *mhsw_server_last_error(const mhsw_server *s);
 /* Uploads and translates the contigs (host pointers), then sizes and starts the slots
  * from what is left of the budget.  Once per server. */
 int mhsw_server_load_contigs(mhsw_server *s, const char *seq, const int64_t *off, const int32_t *len, int64_t count);
-/* Admits a request batch (copied) once the queue budget has room; results go to out5
+/* Admits a request batch once the queue budget has room; results go to out5
  * (5 * n int32: score, a_begin, a_end, b_begin, b_end, B coordinates relative to the
  * window) and win_start (n int64, may be NULL: contig offset of each window) when the
- * ticket completes; both must stay valid until mhsw_server_wait returns. */
+ * ticket completes; they and req->read_seq must stay valid until mhsw_server_wait returns. */
 int mhsw_server_submit(mhsw_server *s, const mhsw_requests *req, int32_t *out5, int64_t *win_start, int flags,
                        uint64_t *ticket);
 /* *done = 1 once the ticket's results are written. */

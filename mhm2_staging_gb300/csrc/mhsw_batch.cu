@@ -245,12 +245,8 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     const int gpb_s = threads / kGKShort, gpb_l = threads / kGKLong;
     const size_t smem_s = (size_t)gpb_s * prof_short, smem_l = (size_t)gpb_l * prof_long;
     cudaError_t e2;
-    if (smem_s > 48 * 1024 && (e2 = cudaFuncSetAttribute(kshort, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         (int)smem_s)))
-      return fail(e2, "smem attribute");
-    if (smem_l > 48 * 1024 && (e2 = cudaFuncSetAttribute(klong, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         (int)smem_l)))
-      return fail(e2, "smem attribute");
+    if ((e2 = raise_smem_limit(reinterpret_cast<const void *>(kshort), smem_s))) return fail(e2, "smem attribute");
+    if ((e2 = raise_smem_limit(reinterpret_cast<const void *>(klong), smem_l))) return fail(e2, "smem attribute");
     int occ_s = 0, occ_l = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, kshort, threads, smem_s);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_l, klong, threads, smem_l);

@@ -15,6 +15,9 @@
 // Output   : k_finalize / k_pack5  -- orientation mapping into the caller's arrays.
 #include <algorithm>
 #include <cstdio>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "mhsw_engine.cuh"
 #include "mhsw_engine16.cuh"
@@ -479,8 +482,8 @@ cudaError_t launch_fwd_t(const FwdConfig &cfg, const PairSet &ps, const ResultSe
                          const int64_t *list, const int *list_count, int ceiling, void *scratch, int scratch_stride,
                          const WorkLists &wl, cudaStream_t st) {
   auto kern = k_fwd<VT, K, kG>;
-  if (cfg.smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+  {
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void *>(kern), cfg.smem);
     if (e != cudaSuccess) return e;
   }
   kern<<<cfg.grid, cfg.groups_per_block * kG, cfg.smem, st>>>(
@@ -493,8 +496,8 @@ template <int K, int G>
 cudaError_t launch_fwd16_t(const FwdConfig &cfg, const PairSet &ps, const ResultSet &rs, const Scoring &sc,
                            int ceiling, void *scratch, int scratch_stride, const WorkLists &wl, cudaStream_t st) {
   auto kern = k_fwd16<K, G>;
-  if (cfg.smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.smem);
+  {
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void *>(kern), cfg.smem);
     if (e != cudaSuccess) return e;
   }
   kern<<<cfg.grid, cfg.groups_per_block * G, cfg.smem, st>>>(ps, rs, sc, ceiling,
@@ -630,12 +633,25 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
   }
   c.grid = std::max(1, std::min(c.grid, sms * 4));
   auto kern = k_rev_wave<4, kG>;
-  if (c.smem > 48 * 1024) {
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem);
-    if (e != cudaSuccess) return e;
-  }
+  e = raise_smem_limit(reinterpret_cast<const void *>(kern), c.smem);
+  if (e != cudaSuccess) return e;
   kern<<<c.grid, c.groups_per_block * kG, c.smem, st>>>(ps, rs, sc, wl, scr, stride, c.pad, c.bcap);
   return cudaGetLastError();
+}
+
+cudaError_t raise_smem_limit(const void *func, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> limit;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &cur = limit[{dev, func}];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
 }
 
 cudaError_t launch_translate(const char *src, uint8_t *dst, int64_t nbytes, cudaStream_t st) {

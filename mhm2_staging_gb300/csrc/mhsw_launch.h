@@ -36,6 +36,12 @@ struct FwdConfig {
 // Upper bound of B length the forward kernels accept (shared-memory code buffer).
 constexpr int kMaxB = 65000;
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` on the current
+// device (no-op at or below the 48 KB default).  The limit only ever grows, so host
+// threads launching the same kernel with different block shapes never lower it under
+// one another's launch.
+cudaError_t raise_smem_limit(const void *func, size_t bytes);
+
 // Chooses K/G/grid/smem for a forward launch over pairs whose A (rows) lengths are at
 // most max_a and B lengths at most max_b.  wide32 selects the int32 engine.
 cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg, bool keyed = false);

@@ -7,8 +7,9 @@
 // window [pos - flank, pos + read_len + flank) clamped to the contig -- the window is an
 // offset into the resident code arena, nothing is copied.
 //
-// Flow.  mhsw_server_submit copies a request batch into host memory and queues it once
-// the queue budget has room (admission).  Each slot -- one driver handle with its own
+// Flow.  mhsw_server_submit computes the windows of a request batch (the read bytes stay
+// in the caller's buffer until its ticket is waited for) and queues it once the queue
+// budget has room (admission).  Each slot -- one driver handle with its own
 // stream and device buffers sized from the device-memory budget -- runs a worker thread
 // that, whenever it is free, packs the waiting pairs (oldest request first, splitting
 // large requests) into one micro-batch, uploads the reads, aligns them against the
@@ -52,8 +53,9 @@ constexpr int32_t kReadBytesPerPair = 256;            // read bytes reserved per
 struct Request {
   uint64_t ticket = 0;
   int32_t n = 0;
-  std::vector<char> seq;        // reads, concatenated
-  std::vector<int64_t> off;     // read offsets into seq (n + 1)
+  const char *src = nullptr;    // the caller's read bytes (valid until the ticket is waited for)
+  std::vector<int64_t> src_off; // read offsets into src
+  std::vector<int64_t> cum;     // prefix sums of the read lengths (n + 1), for packing
   std::vector<int32_t> len;
   std::vector<int64_t> b_off;   // window offsets into the contig code arena
   std::vector<int32_t> b_len;
@@ -175,19 +177,18 @@ int mhsw_server::run_micro_batch(Slot *s, std::vector<Piece> &pieces, int64_t ro
   int64_t ab = 0;
   for (auto &pc : pieces) {
     Request &r = *pc.r;
-    const int64_t o0 = r.off[pc.first], o1 = r.off[pc.first + pc.count];
-    std::memcpy(s->h_seq.p + ab, r.seq.data() + o0, (size_t)(o1 - o0));
     for (int32_t k = 0; k < pc.count; k++) {
       const int32_t i = pc.first + k;
       const int64_t row = pc.row + k;
-      s->h_aoff.p[row] = ab + (r.off[i] - o0);
+      std::memcpy(s->h_seq.p + ab, r.src + r.src_off[i], (size_t)r.len[i]);
+      s->h_aoff.p[row] = ab;
       s->h_alen.p[row] = r.len[i];
       s->h_boff.p[row] = r.b_off[i];
       s->h_blen.p[row] = r.b_len[i];
       max_a = std::max(max_a, r.len[i]);
       max_b = std::max(max_b, r.b_len[i]);
+      ab += r.len[i];
     }
-    ab += o1 - o0;
   }
   (void)bytes;
   cudaStream_t st = s->st;
@@ -239,15 +240,15 @@ void mhsw_server::worker(Slot *s) {
       while (!queue.empty() && rows < slot_pairs) {
         auto r = queue.front();
         int32_t k = 0;
-        const int64_t base = r->off[r->next];
+        const int64_t base = r->cum[r->next];
         while (r->next + k < r->n && rows + k < slot_pairs &&
-               bytes + (r->off[r->next + k + 1] - base) <= slot_read_bytes)
+               bytes + (r->cum[r->next + k + 1] - base) <= slot_read_bytes)
           k++;
         if (k == 0) break;  // the next read does not fit the remaining bytes
         if (r->next == 0) r->t_start = now_s();
         pieces.push_back(Piece{r, r->next, k, rows});
         rows += k;
-        bytes += r->off[r->next + k] - base;
+        bytes += r->cum[r->next + k] - base;
         r->next += k;
         queued_pairs -= k;
         if (r->next == r->n) queue.pop_front();
@@ -473,7 +474,9 @@ int mhsw_server_submit(mhsw_server *s, const mhsw_requests *req, int32_t *out5, 
   r->n = n;
   r->out5 = out5;
   r->win_start = win_start;
-  r->off.resize((size_t)n + 1);
+  r->src = req->read_seq;
+  r->src_off.assign(req->read_off, req->read_off + n);
+  r->cum.resize((size_t)n + 1);
   r->len.resize((size_t)n);
   r->b_off.resize((size_t)n);
   r->b_len.resize((size_t)n);
@@ -489,17 +492,14 @@ int mhsw_server_submit(mhsw_server *s, const mhsw_requests *req, int32_t *out5, 
     if (pos < 0 || pos >= cl) return s->fail(MHSW_ERR_ARG, "read %d: position %d outside contig %d", i, pos, cid);
     const int64_t ws = std::max<int64_t>(0, pos - flank), we = std::min<int64_t>(cl, pos + L + flank);
     if (we - ws > mhsw::kMaxB) return s->fail(MHSW_ERR_LIMIT, "read %d: window of %lld bases", i, (long long)(we - ws));
-    r->off[(size_t)i] = total;
+    r->cum[(size_t)i] = total;
     r->len[(size_t)i] = L;
     r->b_off[(size_t)i] = s->coff[(size_t)cid] + ws;
     r->b_len[(size_t)i] = (int32_t)(we - ws);
     r->wstart[(size_t)i] = ws;
     total += L;
   }
-  r->off[(size_t)n] = total;
-  r->seq.resize((size_t)total);
-  for (int32_t i = 0; i < n; i++)
-    std::memcpy(r->seq.data() + r->off[(size_t)i], req->read_seq + req->read_off[i], (size_t)req->read_len[i]);
+  r->cum[(size_t)n] = total;
   r->bytes = (size_t)total + (size_t)n * 48;
   r->remaining = n;
   r->t_submit = t0;
