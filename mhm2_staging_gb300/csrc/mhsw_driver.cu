@@ -99,7 +99,7 @@ struct mhsw_driver {
   DBuf<int32_t> a_len, b_len;
   DBuf<int32_t> r_score, r_aend, r_bend, r_abeg, r_bbeg;
   DBuf<uint32_t> r_flag;
-  DBuf<int64_t> l_ovf, l_wide, l_esc1, l_esc2;
+  DBuf<int64_t> l_ovf, l_wide, l_bands;
   DBuf<int> l_counts;
   DBuf<uint8_t> a_code, b_code;  // base codes of the current batch
   DBuf<unsigned char> scratch;
@@ -157,8 +157,7 @@ struct mhsw_driver {
     r_flag.release();
     l_ovf.release();
     l_wide.release();
-    l_esc1.release();
-    l_esc2.release();
+    l_bands.release();
     a_code.release();
     b_code.release();
     l_counts.release();
@@ -209,9 +208,8 @@ int ensure_results(mhsw_driver *d, int64_t n) {
   MHSW_CK(d->r_flag.reserve((size_t)n + 1), "cudaMalloc results");
   MHSW_CK(d->l_ovf.reserve((size_t)n + 1), "cudaMalloc lists");
   MHSW_CK(d->l_wide.reserve((size_t)n + 1), "cudaMalloc lists");
-  MHSW_CK(d->l_esc1.reserve((size_t)n + 1), "cudaMalloc lists");
-  MHSW_CK(d->l_esc2.reserve((size_t)n + 1), "cudaMalloc lists");
-  MHSW_CK(d->l_counts.reserve(2 + mhsw::kEscLevels), "cudaMalloc lists");
+  MHSW_CK(d->l_bands.reserve((size_t)n + 1), "cudaMalloc lists");
+  MHSW_CK(d->l_counts.reserve(2 + 2 * mhsw::kBandClasses), "cudaMalloc lists");
   return MHSW_OK;
 }
 
@@ -232,9 +230,8 @@ mhsw::WorkLists work_lists(mhsw_driver *d, int64_t n) {
   wl.wide = d->l_wide.p;
   wl.ovf_count = d->l_counts.p;
   wl.wide_count = d->l_counts.p + 1;
-  wl.esc1 = d->l_esc1.p;
-  wl.esc2 = d->l_esc2.p;
-  wl.esc_counts = d->l_counts.p + 2;
+  wl.bands = d->l_bands.p;
+  wl.band_counts = d->l_counts.p + 2;
   wl.cap = n;
   return wl;
 }
@@ -330,7 +327,7 @@ int run_reverse(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, c
   MHSW_CK(mhsw::launch_reverse(d->device, ps, rs, d->sc, max_a, max_b, d->scratch.p,
                                d->scratch.p ? d->scratch.cap : 0, wl, d->st, order),
           "begin pass launch");
-  d->launches += 8;
+  d->launches += 10;
   return MHSW_OK;
 }
 

@@ -160,13 +160,113 @@ __global__ void __launch_bounds__(256) k_fwd16(PairSet ps, ResultSet rs, Scoring
   }
 }
 
-// One thread per pair: banded begin search (see file header).  The band is WB-1 cells
-// wide (half-width G = WB/2 - 1) and lives in registers, fully unrolled; the codes of a
-// row's band are loaded before its dependency chain starts.  Rows whose band lies
+// Begin pass, banded.  Each pair's search is first assigned a band class: the
+// narrowest instantiation whose half-width holds the gap bound at the first row cap
+// (k_rev_count / k_rev_scatter group the pairs into one segment per class), so every
+// thread of a class kernel has a pair to work on.  One thread per pair: the band is WB-1
+// cells wide (half-width G = WB/2 - 1) and lives in registers, fully unrolled; the codes
+// of a row's band are loaded before its dependency chain starts.  Rows whose band lies
 // inside [0, N2) run without bound checks.  The row cap t starts at 2*score/match + 16
 // and doubles until a row reaches the score, so short low-score alignments stay in a
-// narrow band.  Pairs that need a band wider than this instantiation holds go to
-// out_list for the next wider one.
+// narrow band; a pair whose bound outgrows its class when t doubles goes to the
+// wavefront list.
+__host__ __device__ constexpr int band_half(int c) {  // half-widths 3, 5, 7, 11, 15, 23, 31
+  return c == 0 ? 3 : c == 1 ? 5 : c == 2 ? 7 : c == 3 ? 11 : c == 4 ? 15 : c == 5 ? 23 : 31;
+}
+
+__host__ __device__ __forceinline__ int band_first_cap(int S, int mt, int M2) {
+  const long long tt = 2ll * S / (mt > 0 ? mt : 1) + 16;
+  return (int)(tt < M2 ? tt : M2);
+}
+
+// Total gap length any alignment reaching the score within the first t rows can have:
+// its diagonal steps D <= min(t, N2), so gaps <= (D * match - S) / min(gO, gE).
+// (D <= 65000 and match <= 127 keep the product inside 32 bits.)
+__host__ __device__ __forceinline__ int band_gap_bound(int t, int N2, int S, const Scoring &sc) {
+  const int gmin = sc.gap_open < sc.gap_extend ? sc.gap_open : sc.gap_extend;
+  const int dmax = t < N2 ? t : N2;
+  return (dmax * sc.match - S) / (gmin > 0 ? gmin : 1);
+}
+
+// Band class of pair p (0 .. kBandClasses-1), kBandClasses for the wavefront, or -1 when
+// there is nothing to search (score 0, or a pair the forward pass rejected); those get
+// their begin written here.
+__device__ __forceinline__ int band_class(const ResultSet &rs, const Scoring &sc, int64_t p) {
+  const int S = rs.score[p];
+  if ((rs.flag[p] & kFlagTooLong) || S <= 0) {
+    rs.a_beg[p] = -1;
+    rs.b_beg[p] = 0;
+    return -1;
+  }
+  const int M2 = rs.a_end[p] + 1, N2 = rs.b_end[p] + 1;
+  const int g = band_gap_bound(band_first_cap(S, sc.match, M2), N2, S, sc);
+#pragma unroll
+  for (int c = 0; c < kBandClasses; c++)
+    if (g <= band_half(c)) return c;
+  return kBandClasses;
+}
+
+// Warp-aggregated append of p to list[*count] (one atomic per distinct counter).
+__device__ __forceinline__ void append_agg(int64_t *list, int *count, int64_t cap, int64_t p, bool want) {
+  const unsigned act = __activemask();
+  const unsigned sel = __ballot_sync(act, want);
+  if (!sel) return;
+  const int leader = __ffs(sel) - 1;
+  const int lane32 = threadIdx.x & 31;
+  int base = 0;
+  if (lane32 == leader) base = atomicAdd(count, __popc(sel));
+  base = __shfl_sync(act, base, leader);
+  if (want) {
+    const int slot = base + __popc(sel & ((1u << lane32) - 1u));
+    if (slot < cap) list[slot] = p;
+  }
+}
+
+// Pass 1: count the pairs of each band class.
+__global__ void __launch_bounds__(256) k_rev_count(ResultSet rs, Scoring sc, const uint32_t *__restrict__ order,
+                                                   int64_t n, int *band_counts) {
+  __shared__ int cnt[kBandClasses];
+  if (threadIdx.x < kBandClasses) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = order ? (int64_t)order[idx] : idx;
+    const int c = band_class(rs, sc, p);
+    if (c >= 0 && c < kBandClasses) atomicAdd(&cnt[c], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x < kBandClasses && cnt[threadIdx.x]) atomicAdd(&band_counts[threadIdx.x], cnt[threadIdx.x]);
+}
+
+// Pass 2: place each pair in its class segment (segments in class order, each filled in
+// the batch's order); wider pairs go to the wavefront list.
+__global__ void __launch_bounds__(256) k_rev_scatter(ResultSet rs, Scoring sc, const uint32_t *__restrict__ order,
+                                                     int64_t n, WorkLists wl) {
+  int off[kBandClasses];
+  int acc = 0;
+#pragma unroll
+  for (int c = 0; c < kBandClasses; c++) {
+    off[c] = acc;
+    acc += wl.band_counts[c];
+  }
+  int *cursor = wl.band_counts + kBandClasses;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = order ? (int64_t)order[idx] : idx;
+    const int S = rs.score[p];
+    int c = -1;
+    if (!((rs.flag[p] & kFlagTooLong) || S <= 0)) {
+      const int M2 = rs.a_end[p] + 1, N2 = rs.b_end[p] + 1;
+      const int g = band_gap_bound(band_first_cap(S, sc.match, M2), N2, S, sc);
+      c = kBandClasses;
+#pragma unroll
+      for (int k = kBandClasses - 1; k >= 0; k--)
+        if (g <= band_half(k)) c = k;
+    }
+    append_agg(wl.wide, wl.wide_count, wl.cap, p, c == kBandClasses);
+#pragma unroll
+    for (int k = 0; k < kBandClasses; k++) append_agg(wl.bands + off[k], cursor + k, wl.cap - off[k], p, c == k);
+  }
+}
+
 template <int WB>
 __device__ __forceinline__ void band_row(const uint8_t *__restrict__ b, int i, int N2, uint32_t rp0, uint32_t rp1,
                                          int gO, int gE, int (&H)[WB], int (&E)[WB], int &rowmax, bool edge) {
@@ -206,53 +306,45 @@ __device__ __forceinline__ void band_row(const uint8_t *__restrict__ b, int i, i
   rowmax = rm;
 }
 
-template <int WB>
-__global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scoring sc,
-                                                  const uint32_t *__restrict__ order,
-                                                  const int64_t *__restrict__ in_list, const int *__restrict__ in_count,
-                                                  int64_t *out_list, int *out_count, int64_t cap) {
+// Pass 3 (one launch per class C): the banded search over the class's segment.
+template <int WB, int C>
+__global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl) {
   constexpr int NEG = -(1 << 28);
   constexpr int G = WB / 2 - 1;
   constexpr int W = 2 * G + 1;
+  static_assert(G == band_half(C), "band class and width disagree");
   const int gO = sc.gap_open, gE = sc.gap_extend, mt = sc.match;
-  const int gmin = gO < gE ? gO : gE;
-  int64_t total = ps.n;
-  if (in_list) {
-    total = *in_count;
-    if (total > cap) total = cap;
-  }
+  int64_t off = 0;
+#pragma unroll
+  for (int c = 0; c < C; c++) off += wl.band_counts[c];
+  int64_t total = wl.band_counts[C];
+  if (off + total > wl.cap) total = wl.cap - off;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = in_list ? in_list[idx] : (order ? (int64_t)order[idx] : idx);
+    const int64_t p = wl.bands[off + idx];
     const int S = rs.score[p];
-    if (!in_list && ((rs.flag[p] & kFlagTooLong) || S <= 0)) {
-      rs.a_beg[p] = -1;
-      rs.b_beg[p] = 0;
-      continue;
-    }
     const int ie = rs.a_end[p], je = rs.b_end[p];
     const int M2 = ie + 1, N2 = je + 1;
     const uint8_t *a = ps.a_code + ps.a_off[p] + ie;  // reversed: a[-i]
     const uint8_t *b = ps.b_code + ps.b_off[p] + je;  // reversed: b[-j]
-    long long tt = 2ll * S / (mt > 0 ? mt : 1) + 16;
-    int t = (int)(tt < M2 ? tt : M2);
+    int t = band_first_cap(S, mt, M2);
     int fi = -1, fj = -1;
     bool escalate = false, found = false;
+    int H[W + 1], E[W + 1];
+#pragma unroll
+    for (int d = 0; d <= W; d++) {
+      H[d] = 0;
+      E[d] = NEG;
+    }
+    // The band is the same for every row cap, so a longer cap continues from the row
+    // the previous one stopped at.
+    int i = 0;
     for (;;) {
-      // diagonal steps D <= min(rows, columns) of the box; gaps total <= (D*match - S)/gmin
-      const long long dmax = t < N2 ? t : N2;
-      long long g = (dmax * mt - S) / (gmin > 0 ? gmin : 1);
-      if (g > G) {
+      if (band_gap_bound(t, N2, S, sc) > G) {
         escalate = true;
         break;
       }
-      int H[W + 1], E[W + 1];
-#pragma unroll
-      for (int d = 0; d <= W; d++) {
-        H[d] = 0;
-        E[d] = NEG;
-      }
-      for (int i = 0; i < t; i++) {
+      for (; i < t; i++) {
         const int ca = a[-i];
         uint32_t rp0 = 0, rp1 = 0;  // s(ca, cb) + 128 as bytes 0..4 of {rp0, rp1}
 #pragma unroll
@@ -282,20 +374,7 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
       if (found || t >= M2) break;
       t = (2 * t < M2) ? 2 * t : M2;
     }
-    // warp-aggregated append of the pairs that need a wider band
-    const unsigned act = __activemask();
-    const unsigned esc = __ballot_sync(act, escalate);
-    if (esc) {
-      const int leader = __ffs(esc) - 1;
-      const int lane32 = threadIdx.x & 31;
-      int base = 0;
-      if (lane32 == leader) base = atomicAdd(out_count, __popc(esc));
-      base = __shfl_sync(act, base, leader);
-      if (escalate) {
-        const int slot = base + __popc(esc & ((1u << lane32) - 1u));
-        if (slot < cap) out_list[slot] = p;
-      }
-    }
+    append_agg(wl.wide, wl.wide_count, wl.cap, p, escalate);
     if (escalate) continue;
     if (!found) {
       rs.flag[p] |= kFlagTooLong;  // inconsistent; reported as an error by the driver
@@ -438,7 +517,7 @@ __global__ void k_pack5(ResultSet rs, int64_t n, int32_t *out5) {
 __global__ void k_reset_lists(WorkLists wl) {
   *wl.ovf_count = 0;
   *wl.wide_count = 0;
-  for (int i = 0; i < kEscLevels; i++) wl.esc_counts[i] = 0;
+  for (int i = 0; i < 2 * kBandClasses; i++) wl.band_counts[i] = 0;
 }
 
 int g_num_sms = 0;
@@ -593,26 +672,19 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
                            const uint32_t *order) {
   const int sms = num_sms(device);
   if (ps.n > 0) {
-    const int64_t blocks = (ps.n + 127) / 128;
-    const int grid = (int)std::min<int64_t>(blocks, (int64_t)sms * 16);
-    const int gridl = sms * 8;
-    // Band classes 7, 11, 15, 23, 31, 47, 63 cells; each kernel passes the pairs that need
-    // a wider band to the next one through alternating lists (esc1, esc2) with one
-    // counter per level (esc_counts[0..6]); the last level feeds wl.wide.
-    int64_t *lists[2] = {wl.esc1, wl.esc2};
-    k_rev_band<8><<<grid, 128, 0, st>>>(ps, rs, sc, order, nullptr, nullptr, lists[0], wl.esc_counts + 0, wl.cap);
-    k_rev_band<12><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[0], wl.esc_counts + 0, lists[1],
-                                          wl.esc_counts + 1, wl.cap);
-    k_rev_band<16><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[1], wl.esc_counts + 1, lists[0],
-                                          wl.esc_counts + 2, wl.cap);
-    k_rev_band<24><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[0], wl.esc_counts + 2, lists[1],
-                                          wl.esc_counts + 3, wl.cap);
-    k_rev_band<32><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[1], wl.esc_counts + 3, lists[0],
-                                          wl.esc_counts + 4, wl.cap);
-    k_rev_band<48><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[0], wl.esc_counts + 4, lists[1],
-                                          wl.esc_counts + 5, wl.cap);
-    k_rev_band<64><<<gridl, 128, 0, st>>>(ps, rs, sc, nullptr, lists[1], wl.esc_counts + 5, wl.wide, wl.wide_count,
-                                          wl.cap);
+    const int grid = (int)std::min<int64_t>((ps.n + 255) / 256, (int64_t)sms * 8);
+    const int gridb = sms * 8;
+    // band classes by half-width 3, 5, 7, 11, 15, 23, 31 (band of 7 .. 63 cells); the
+    // segments' counts stay on the device.
+    k_rev_count<<<grid, 256, 0, st>>>(rs, sc, order, ps.n, wl.band_counts);
+    k_rev_scatter<<<grid, 256, 0, st>>>(rs, sc, order, ps.n, wl);
+    k_rev_band<8, 0><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
+    k_rev_band<12, 1><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
+    k_rev_band<16, 2><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
+    k_rev_band<24, 3><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
+    k_rev_band<32, 4><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
+    k_rev_band<48, 5><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
+    k_rev_band<64, 6><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

@@ -9,7 +9,7 @@ struct Scoring;
 struct PairSet;
 struct ResultSet;
 
-constexpr int kEscLevels = 8;
+constexpr int kBandClasses = 7;  // banded begin-pass instantiations (half-widths 3 .. 31)
 
 // Work lists built on the device (no host round trip between passes).
 struct WorkLists {
@@ -17,8 +17,8 @@ struct WorkLists {
   int *ovf_count;
   int64_t *wide;      // pairs whose reverse band is wider than the banded kernels handle
   int *wide_count;
-  int64_t *esc1, *esc2;  // alternating escalation lists between the banded begin kernels
-  int *esc_counts;       // kEscLevels counters, one per band level
+  int64_t *bands;     // begin-pass pairs grouped by band class (one segment per class)
+  int *band_counts;   // kBandClasses pair counts, then kBandClasses scatter cursors
   int64_t cap;        // capacity of each list
 };
 
