@@ -185,7 +185,8 @@ void BatchState::release() {
 }
 
 int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultSet &rs, const WorkLists &wl,
-                    const Scoring &sc, int ceiling, int max_a, int max_b, cudaStream_t st, int64_t *launches) {
+                    const Scoring &sc, int ceiling, int max_a, int max_b, cudaStream_t st, int64_t *launches,
+                    const Forks *fk) {
   auto fail = [&](cudaError_t e, const char *what) {
     bs.err = std::string(what) + ": " + cudaGetErrorString(e);
     return 1;
@@ -276,12 +277,15 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     }
     cudaMemsetAsync(bs.queue, 0, 2 * sizeof(int), st);
     cudaMemsetAsync(wl.ovf_count, 0, sizeof(int), st);
+    const bool fan = fk && fk->fork;
+    if (fan && (e2 = fork_to(*fk, st, 1))) return fail(e2, "fork");
+    klong<<<grid_l, threads, smem_l, fan ? fk->side[0] : st>>>(ps, rs, sc, bs.keys_out, bs.idx_out, n, bs.queue,
+                                                               bs.queue + 2, ceiling, wl, pad, bcap, scr, stride);
     kshort<<<grid_s, threads, smem_s, st>>>(ps, rs, sc, bs.keys_out, bs.idx_out, n, bs.queue, bs.queue + 2, ceiling,
                                              wl, pad, bcap, nullptr, stride);
-    klong<<<grid_l, threads, smem_l, st>>>(ps, rs, sc, bs.keys_out, bs.idx_out, n, bs.queue, bs.queue + 2, ceiling,
-                                           wl, pad, bcap, scr, stride);
     e2 = cudaGetLastError();
     if (e2) return fail(e2, "persistent forward launch");
+    if (fan && (e2 = join_from(*fk, st, 1))) return fail(e2, "join");
     if (launches) *launches += 2;
     if (ms) {
       cudaEventRecord(t1, st);

@@ -9,6 +9,7 @@
 namespace mhsw {
 
 struct WorkLists;
+struct Forks;
 
 // One tuned launch shape of the persistent kernel.
 struct BatchShape {
@@ -39,7 +40,10 @@ struct BatchState {
 // persistent kernel whose lane groups claim pairs from one atomic queue.  Pairs whose
 // score could exceed the int16 ceiling go straight to the int32 list wl.ovf.
 // The first call tunes the launch shape (groups per block, blocks per SM) on the batch.
+// With side streams (fk), the two persistent launches (8-lane and 16-lane groups) run
+// concurrently, so the tail of one fills with the other.
 int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultSet &rs, const WorkLists &wl,
-                    const Scoring &sc, int ceiling, int max_a, int max_b, cudaStream_t st, int64_t *launches);
+                    const Scoring &sc, int ceiling, int max_a, int max_b, cudaStream_t st, int64_t *launches,
+                    const Forks *fk = nullptr);
 
 }  // namespace mhsw

@@ -106,6 +106,7 @@ struct mhsw_driver {
   DBuf<unsigned char> outv;  // 5 x int16 + 5 x int32 arrays
   DBuf<int32_t> out5;
   mhsw::BatchState batch;     // batched-form work buffers
+  mhsw::Forks forks;          // side streams for launches that overlap on the device
 
   // pinned host staging
   HBuf<char> h_a, h_b;
@@ -173,6 +174,7 @@ struct mhsw_driver {
     h_blen.release();
     h_outv.release();
     h_counts.release();
+    mhsw::forks_destroy(forks);
     for (auto &e : ev_t)
       if (e) cudaEventDestroy(e);
     if (ev_done) cudaEventDestroy(ev_done);
@@ -303,7 +305,7 @@ int forward_any(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, i
   MHSW_CK(mhsw::reset_lists(wl, d->st), "reset lists");
   d->launches += 1;
   if (mhsw::batched_forward(d->batch, d->device, ps, result_set(d), wl, d->sc, ceiling_for(d), max_a, max_b, d->st,
-                            &d->launches))
+                            &d->launches, &d->forks))
     return d->fail(MHSW_ERR_CUDA, "batched forward: %s", d->batch.err.c_str());
   d->fwd_order = d->batch.idx_out;
   // int32 pass over the pairs the int16 engine could not hold
@@ -325,7 +327,7 @@ int run_reverse(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, c
   mhsw::ResultSet rs = result_set(d);
   mhsw::WorkLists wl = work_lists(d, ps.n);
   MHSW_CK(mhsw::launch_reverse(d->device, ps, rs, d->sc, max_a, max_b, d->scratch.p,
-                               d->scratch.p ? d->scratch.cap : 0, wl, d->st, order),
+                               d->scratch.p ? d->scratch.cap : 0, wl, d->st, order, &d->forks),
           "begin pass launch");
   d->launches += 10;
   return MHSW_OK;
@@ -551,6 +553,7 @@ int mhsw_driver_init(mhsw_driver *d, int rank_me, int rank_n, short match_score,
   MHSW_CK(cudaSetDevice(d->device), "cudaSetDevice");
   MHSW_CK(cudaStreamCreateWithFlags(&d->st, cudaStreamNonBlocking), "cudaStreamCreate");
   MHSW_CK(cudaEventCreateWithFlags(&d->ev_done, cudaEventDisableTiming), "cudaEventCreate");
+  MHSW_CK(mhsw::forks_create(d->forks), "side streams");
   for (auto &e : d->ev_t) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
   d->sc = s;
   d->inited = true;

@@ -267,53 +267,59 @@ __global__ void __launch_bounds__(256) k_rev_scatter(ResultSet rs, Scoring sc, c
   }
 }
 
-template <int WB>
-__device__ __forceinline__ void band_row(const uint8_t *__restrict__ b, int i, int N2, uint32_t rp0, uint32_t rp1,
-                                         int gO, int gE, int (&H)[WB], int (&E)[WB], int &rowmax, bool edge) {
+// One band row: W cells, dependency chain along the row through F.  Gap values are kept
+// biased by +gO (E^ = E + gO, F^ = F + gO) so H feeds their updates directly.  cb[u + d]
+// holds the code of band cell d's column OR 0x7770 (a byte_perm selector: byte 0 picks
+// the row's score for that code, bytes 1-3 read zero); columns outside [0, N2) carry the
+// PAD code, which scores -128: cells left of column 0 then stay exactly at the boundary
+// values and cells right of the last column stay below the score, so the band needs no
+// per-cell bound checks.
+template <int W, int NC>
+__device__ __forceinline__ int band_row(const int (&cb)[NC], int u, uint32_t rp0, uint32_t rp1, int bias, int ngo,
+                                        int nge, int (&H)[W + 1], int (&E)[W + 1]) {
   constexpr int NEG = -(1 << 28);
-  constexpr int G = WB / 2 - 1;
-  constexpr int W = 2 * G + 1;
-  const int jlo = i - G;
-  int cb[W];
-#pragma unroll
-  for (int d = 0; d < W; d++) {
-    int j = jlo + d;
-    if (edge) j = j < 0 ? 0 : (j >= N2 ? N2 - 1 : j);
-    cb[d] = b[-j];
-  }
   int F = NEG;
   int rm = 0;
 #pragma unroll
   for (int d = 0; d < W; d++) {
-    const int s = (int)__byte_perm(rp0, rp1, 0x7770u | (uint32_t)cb[d]) - 128;
-    const int e = __viaddmax_s32(E[d + 1], -gE, H[d + 1] - gO);
-    int h = __vimax3_s32_relu(H[d] + s, e, F);
-    int f = __viaddmax_s32(F, -gE, h - gO);
-    if (edge) {
-      const int j = jlo + d;
-      const bool left = j < 0;
-      h = left ? 0 : h;
-      E[d] = left ? NEG : e;
-      F = left ? -gO : f;
-      rm = (j < N2) ? max(rm, h) : rm;
-    } else {
-      E[d] = e;
-      F = f;
-      rm = max(rm, h);
-    }
+    const int q = H[d] + (int)__byte_perm(rp0, rp1, (uint32_t)cb[u + d]) + bias;  // Hdiag + s + gO
+    const int e = __viaddmax_s32(E[d + 1], nge, H[d + 1]);
+    const int h = __viaddmax_s32_relu(__vimax3_s32(q, e, F), ngo, 0);
+    F = __viaddmax_s32(F, nge, h);
+    E[d] = e;
     H[d] = h;
+    rm = max(rm, h);
   }
-  rowmax = rm;
+  return rm;
 }
 
-// Pass 3 (one launch per class C): the banded search over the class's segment.
+// Pass 3 (one launch per class C): the banded search over the class's segment.  Rows go
+// in blocks of U; the band's codes live in a register window of W + U columns that
+// slides by U columns per block (one load per new column), and the row's scores come from
+// a per-block table indexed by the A code.
 template <int WB, int C>
 __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl) {
   constexpr int NEG = -(1 << 28);
   constexpr int G = WB / 2 - 1;
   constexpr int W = 2 * G + 1;
+  constexpr int U = W <= 15 ? 8 : (W <= 31 ? 4 : 2);
+  constexpr int NC = W + U;
   static_assert(G == band_half(C), "band class and width disagree");
-  const int gO = sc.gap_open, gE = sc.gap_extend, mt = sc.match;
+  __shared__ uint32_t rptab[2 * 8];  // per A code 0..4: s(a, c) + 128 as bytes c = 0..3 | c = 4, PAD
+  if (threadIdx.x < 5) {
+    const int a = threadIdx.x;
+    uint32_t r0 = 0, r1 = 0;
+    for (int c = 0; c < 5; c++) {
+      const uint32_t v = (uint32_t)(sub_score(a, c, sc, 128) + 128) & 0xffu;
+      if (c < 4) r0 |= v << (8 * c);
+      else r1 = v;  // byte 1 (PAD) and above stay 0: score -128
+    }
+    rptab[2 * a] = r0;
+    rptab[2 * a + 1] = r1;
+  }
+  __syncthreads();
+  const int mt = sc.match;
+  const int bias = sc.gap_open - 128, ngo = -sc.gap_open, nge = -sc.gap_extend;
   int64_t off = 0;
 #pragma unroll
   for (int c = 0; c < C; c++) off += wl.band_counts[c];
@@ -327,52 +333,56 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
     const int M2 = ie + 1, N2 = je + 1;
     const uint8_t *a = ps.a_code + ps.a_off[p] + ie;  // reversed: a[-i]
     const uint8_t *b = ps.b_code + ps.b_off[p] + je;  // reversed: b[-j]
-    int t = band_first_cap(S, mt, M2);
+    auto code_at = [&](int j) -> int { return ((unsigned)j < (unsigned)N2 ? (int)b[-j] : kCodePad) | 0x7770; };
+    // row caps are kept at multiples of U (or M2) so the window always slides by U
+    auto cap_rows = [&](int t) { t = (t + U - 1) / U * U; return t < M2 ? t : M2; };
+    int t = cap_rows(band_first_cap(S, mt, M2));
     int fi = -1, fj = -1;
     bool escalate = false, found = false;
-    int H[W + 1], E[W + 1];
+    int H[W + 1], E[W + 1], cb[NC];
 #pragma unroll
     for (int d = 0; d <= W; d++) {
       H[d] = 0;
       E[d] = NEG;
     }
-    // The band is the same for every row cap, so a longer cap continues from the row
-    // the previous one stopped at.
-    int i = 0;
+#pragma unroll
+    for (int k = 0; k < NC; k++) cb[k] = code_at(k - G);
+    int i = 0;  // first row of the current block; the window covers columns i - G + [0, NC)
     for (;;) {
       if (band_gap_bound(t, N2, S, sc) > G) {
         escalate = true;
         break;
       }
-      for (; i < t; i++) {
-        const int ca = a[-i];
-        uint32_t rp0 = 0, rp1 = 0;  // s(ca, cb) + 128 as bytes 0..4 of {rp0, rp1}
+      while (i < t && !found) {
 #pragma unroll
-        for (int c = 0; c < 5; c++) {
-          const uint32_t v = (uint32_t)(sub_score(ca, c, sc, 1 << 20) + 128) & 0xffu;
-          if (c < 4) rp0 |= v << (8 * c);
-          else rp1 = v;
-        }
-        int rowmax;
-        const bool edge = (i - G < 0) || (i + G >= N2);
-        if (edge) band_row<W + 1>(b, i, N2, rp0, rp1, gO, gE, H, E, rowmax, true);
-        else band_row<W + 1>(b, i, N2, rp0, rp1, gO, gE, H, E, rowmax, false);
-        if (rowmax >= S) {
-          // first cell of this row that reaches the score
+        for (int u = 0; u < U; u++) {
+          const int row = i + u;
+          if (!found && row < t) {
+            const int ca = a[-row];
+            const int rm = band_row<W, NC>(cb, u, rptab[2 * ca], rptab[2 * ca + 1], bias, ngo, nge, H, E);
+            if (rm >= S) {
+              // first cell of this row that reaches the score
 #pragma unroll
-          for (int d = 0; d < W; d++) {
-            const int j = i - G + d;
-            if (!found && j >= 0 && j < N2 && H[d] >= S) {
-              found = true;
-              fi = i;
-              fj = j;
+              for (int d = 0; d < W; d++) {
+                const int j = row - G + d;
+                if (!found && j >= 0 && j < N2 && H[d] >= S) {
+                  found = true;
+                  fi = row;
+                  fj = j;
+                }
+              }
             }
           }
-          break;
         }
+        if (found || i + U >= M2) break;
+        i += U;
+#pragma unroll
+        for (int k = 0; k < W; k++) cb[k] = cb[k + U];
+#pragma unroll
+        for (int k = W; k < NC; k++) cb[k] = code_at(i - G + k);
       }
       if (found || t >= M2) break;
-      t = (2 * t < M2) ? 2 * t : M2;
+      t = cap_rows(2 * t);
     }
     append_agg(wl.wide, wl.wide_count, wl.cap, p, escalate);
     if (escalate) continue;
@@ -667,9 +677,44 @@ cudaError_t launch_forward(const FwdConfig &cfg, bool wide32, const PairSet &ps,
   }
 }
 
+cudaError_t forks_create(Forks &f) {
+  cudaError_t e = cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming);
+  for (int k = 0; k < kSideStreams && e == cudaSuccess; k++) {
+    e = cudaStreamCreateWithFlags(&f.side[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.join[k], cudaEventDisableTiming);
+  }
+  return e;
+}
+
+void forks_destroy(Forks &f) {
+  for (int k = 0; k < kSideStreams; k++) {
+    if (f.side[k]) cudaStreamDestroy(f.side[k]);
+    if (f.join[k]) cudaEventDestroy(f.join[k]);
+    f.side[k] = nullptr;
+    f.join[k] = nullptr;
+  }
+  if (f.fork) cudaEventDestroy(f.fork);
+  f.fork = nullptr;
+}
+
+cudaError_t fork_to(const Forks &f, cudaStream_t st, int k) {
+  cudaError_t e = cudaEventRecord(f.fork, st);
+  for (int i = 0; i < k && e == cudaSuccess; i++) e = cudaStreamWaitEvent(f.side[i], f.fork, 0);
+  return e;
+}
+
+cudaError_t join_from(const Forks &f, cudaStream_t st, int k) {
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < k && e == cudaSuccess; i++) {
+    e = cudaEventRecord(f.join[i], f.side[i]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, f.join[i], 0);
+  }
+  return e;
+}
+
 cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, const Scoring &sc, int max_a,
                            int max_b, void *scratch, size_t scratch_bytes, const WorkLists &wl, cudaStream_t st,
-                           const uint32_t *order) {
+                           const uint32_t *order, const Forks *fk) {
   const int sms = num_sms(device);
   if (ps.n > 0) {
     const int grid = (int)std::min<int64_t>((ps.n + 255) / 256, (int64_t)sms * 8);
@@ -678,15 +723,28 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
     // segments' counts stay on the device.
     k_rev_count<<<grid, 256, 0, st>>>(rs, sc, order, ps.n, wl.band_counts);
     k_rev_scatter<<<grid, 256, 0, st>>>(rs, sc, order, ps.n, wl);
-    k_rev_band<8, 0><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
-    k_rev_band<12, 1><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
-    k_rev_band<16, 2><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
-    k_rev_band<24, 3><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
-    k_rev_band<32, 4><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
-    k_rev_band<48, 5><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
-    k_rev_band<64, 6><<<gridb, 128, 0, st>>>(ps, rs, sc, wl);
+    // The classes are independent: with side streams they run concurrently, so the
+    // latency-bound narrow classes share the SMs with the wide ones.
+    cudaStream_t cs[kBandClasses];
+    const bool fan = fk && fk->fork;
+    if (fan) {
+      cudaError_t e = fork_to(*fk, st, kBandClasses);
+      if (e != cudaSuccess) return e;
+    }
+    for (int c = 0; c < kBandClasses; c++) cs[c] = fan ? fk->side[c] : st;
+    k_rev_band<64, 6><<<gridb, 128, 0, cs[6]>>>(ps, rs, sc, wl);
+    k_rev_band<48, 5><<<gridb, 128, 0, cs[5]>>>(ps, rs, sc, wl);
+    k_rev_band<32, 4><<<gridb, 128, 0, cs[4]>>>(ps, rs, sc, wl);
+    k_rev_band<24, 3><<<gridb, 128, 0, cs[3]>>>(ps, rs, sc, wl);
+    k_rev_band<16, 2><<<gridb, 128, 0, cs[2]>>>(ps, rs, sc, wl);
+    k_rev_band<12, 1><<<gridb, 128, 0, cs[1]>>>(ps, rs, sc, wl);
+    k_rev_band<8, 0><<<gridb, 128, 0, cs[0]>>>(ps, rs, sc, wl);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (fan) {
+      e = join_from(*fk, st, kBandClasses);
+      if (e != cudaSuccess) return e;
+    }
   }
   // Wide bands: wavefront on the reversed box (count read on the device).
   FwdConfig c;

@@ -36,6 +36,23 @@ struct FwdConfig {
 // Upper bound of B length the forward kernels accept (shared-memory code buffer).
 constexpr int kMaxB = 65000;
 
+// Side streams of one driver handle, for launches that may overlap on the device (the
+// two persistent forward launches; the band classes of the begin pass).  Work forked
+// onto them waits for everything issued on the main stream before the fork, and the
+// main stream waits for all of it at the join, so the main stream's order is kept.
+constexpr int kSideStreams = 8;
+struct Forks {
+  cudaStream_t side[kSideStreams] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[kSideStreams] = {};
+};
+cudaError_t forks_create(Forks &f);
+void forks_destroy(Forks &f);
+// Side streams 0 .. k-1 wait for the work issued so far on st.
+cudaError_t fork_to(const Forks &f, cudaStream_t st, int k);
+// st waits for the work issued so far on side streams 0 .. k-1.
+cudaError_t join_from(const Forks &f, cudaStream_t st, int k);
+
 // Raises a kernel's dynamic shared-memory limit to at least `bytes` on the current
 // device (no-op at or below the 48 KB default).  The limit only ever grows, so host
 // threads launching the same kernel with different block shapes never lower it under
@@ -64,7 +81,7 @@ bool keyed_scoring(const Scoring &sc);
 // left in wl.wide.  order (may be null) is the pair order of the first kernel.
 cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, const Scoring &sc, int max_a,
                            int max_b, void *scratch, size_t scratch_bytes, const WorkLists &wl, cudaStream_t st,
-                           const uint32_t *order);
+                           const uint32_t *order, const Forks *fk = nullptr);
 
 // Raw bytes -> base codes (0..4) for one arena.
 cudaError_t launch_translate(const char *src, uint8_t *dst, int64_t nbytes, cudaStream_t st);
