@@ -72,7 +72,10 @@ typedef struct {
   int64_t n_pairs;
   int64_t n_overflow16;  /* pairs re-run in int32 */
   int64_t n_rev_wide;    /* begin searches that used the wavefront path */
-  int64_t launches;      /* kernels launched by the call */
+  int64_t launches;      /* kernels launched by the call (a graph replay counts its kernels) */
+  int64_t graph_replays; /* CUDA graph launches by this handle so far: a device-resident batch
+                          * aligned again with the same pointers, sizes and settings is
+                          * captured on its second call and replayed from then on */
 } mhsw_timing;
 
 typedef struct {
@@ -93,11 +96,11 @@ typedef struct {
   const int64_t *b_off;
   const int32_t *b_len;
   int64_t n;
-  /* Optional hints for device-resident batches (0 = unknown): the longest A and B,
-   * the sum of len(A)*len(B), and the byte extents of the two arenas
-   * (max over pairs of off + len).  With all four of max_a_len, max_b_len, a_bytes
-   * and b_bytes given, a device batch is launched without reading its lengths or
-   * offsets back to the host. */
+  /* Optional hints (0 = unknown): the longest A and B, the sum of len(A)*len(B), and
+   * the byte extents of the two arenas (max over pairs of off + len).  With all four of
+   * max_a_len, max_b_len, a_bytes and b_bytes given, a device batch is launched without
+   * reading its lengths or offsets back, and a host batch without scanning them on the
+   * host; the caller then vouches that they bound every pair. */
   int32_t max_a_len;
   int32_t max_b_len;
   double cells;

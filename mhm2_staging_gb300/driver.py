@@ -54,6 +54,7 @@ class Timing(C.Structure):
         ("n_overflow16", C.c_int64),
         ("n_rev_wide", C.c_int64),
         ("launches", C.c_int64),
+        ("graph_replays", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -391,13 +392,17 @@ class GPUDriver:
             arr(r.top_scores32, np.int32))
 
     # ---- batch entry point ---------------------------------------------------------
-    def align_pairs(self, pairs: "Pairs", form: int = FORM_PLAIN, out: np.ndarray | None = None) -> np.ndarray:
+    def align_pairs(self, pairs: "Pairs", form: int = FORM_PLAIN, out: np.ndarray | None = None,
+                    hints: bool = False) -> np.ndarray:
         """Aligns host-resident pairs (A = SSW ref, B = SSW query); returns n x 5 int32
-        (score, a_begin, a_end, b_begin, b_end)."""
+        (score, a_begin, a_end, b_begin, b_end).  hints=True passes the batch's extents
+        (from Pairs.extents(), computed once per batch) so the call skips its host scan."""
         n = pairs.n
         if out is None:
             out = np.zeros((n, 5), dtype=np.int32)
         pt = pairs.c_struct()
+        if hints:
+            pt.max_a_len, pt.max_b_len, pt.cells, pt.a_bytes, pt.b_bytes = pairs.extents()
         self._ck(self._lib.mhsw_align_pairs(self._h, C.byref(pt), out.ctypes.data_as(_P) if n else None, 1, form),
                  "align_pairs")
         return out
@@ -431,6 +436,19 @@ class Pairs:
 
     def cells(self) -> int:
         return int((self.a_len.astype(np.int64) * self.b_len.astype(np.int64)).sum())
+
+    def extents(self) -> tuple[int, int, float, int, int]:
+        """(longest A, longest B, cells, A arena bytes, B arena bytes), cached."""
+        ext = getattr(self, "_extents", None)
+        if ext is None or ext[0] != self.n:
+            if self.n == 0:
+                vals = (0, 0, 0.0, 0, 0)
+            else:
+                vals = (int(self.a_len.max()), int(self.b_len.max()), float(self.cells()),
+                        int((self.a_off + self.a_len).max()), int((self.b_off + self.b_len).max()))
+            ext = (self.n, vals)
+            object.__setattr__(self, "_extents", ext)
+        return ext[1]
 
     def c_struct(self) -> PairsT:
         for arr, dt in ((self.a_seq, np.uint8), (self.b_seq, np.uint8), (self.a_off, np.int64),

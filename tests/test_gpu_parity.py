@@ -108,3 +108,40 @@ def test_single_pair_and_empty_batch(gpu):
     assert not _diff(gpu.align_pairs(p), oracle.align_batch(p, SC))
     e = Pairs.from_lists([], [])
     assert gpu.align_pairs(e).shape == (0, 5)
+
+
+@pytest.mark.parametrize("form", [FORM_PLAIN, FORM_BATCHED])
+def test_repeated_device_batch_replays_a_cuda_graph(built, form):
+    """The same device-resident batch aligned repeatedly: the second call is captured into
+    a CUDA graph and later calls replay it; every call gives the oracle's results."""
+    torch = pytest.importorskip("torch")
+    from mhm2_staging_gb300.driver import DevicePairs
+
+    pairs = workloads.generate(2, n=30000, first=4242)
+    want = oracle.align_batch(pairs, SC)
+    dev = torch.device("cuda:0")
+    tens = [torch.from_numpy(x).to(dev) for x in (pairs.a_seq, pairs.a_off, pairs.a_len, pairs.b_seq, pairs.b_off,
+                                                 pairs.b_len)]
+    dp = DevicePairs(*(t.data_ptr() for t in tens), n=pairs.n, max_a_len=int(pairs.a_len.max()),
+                     max_b_len=int(pairs.b_len.max()), cells=float(pairs.cells()),
+                     a_bytes=int((pairs.a_off + pairs.a_len).max()), b_bytes=int((pairs.b_off + pairs.b_len).max()))
+    d = GPUDriver()
+    d.init(0, 1, 1, -3, -5, -2, 0)
+    d.set_ambiguity(-2)
+    out = torch.full((pairs.n, 5), -9, dtype=torch.int32, device=dev)
+    replays = []
+    for call in range(4):
+        out.fill_(-9)
+        torch.cuda.synchronize()
+        d.align_pairs_device(dp, out.data_ptr(), form=form)
+        got = out.cpu().numpy()
+        assert not _diff(got, want, pairs), f"call {call}"
+        replays.append(d.last_timing()["graph_replays"])
+    assert replays == [0, 1, 2, 3], replays
+
+
+def test_host_batch_with_stated_extents(gpu):
+    pairs = workloads.generate(1, n=5000, first=777)
+    want = oracle.align_batch(pairs, SC)
+    got = gpu.align_pairs(pairs, form=FORM_BATCHED, hints=True)
+    assert not _diff(got, want, pairs)
