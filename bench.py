@@ -217,6 +217,54 @@ def run_serving(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_paths(drv, dev, torch, stream) -> dict:
+    """GCUPS of the other measured workloads on the same driver, inputs resident on the
+    device (each: 2 warm-up calls, then 3 timed with CUDA events on the driver's stream):
+    the 150/300 bp batch (plain and batched form), the 1M-pair read/ref mix with 30%
+    unrelated reads, the 200k long-reference batch, and the 200k-pair slice of the uneven
+    batch with every pair re-run by the int32 engine (int16 ceiling 0)."""
+    from mhm2_staging_gb300 import FORM_BATCHED, FORM_PLAIN, workloads
+    from mhm2_staging_gb300.driver import DevicePairs, limits
+
+    out = {}
+    specs = [("150bp_vs_300bp_10k_pairs_plain", 0, 10_000, FORM_PLAIN, None),
+             ("150bp_vs_300bp_10k_pairs_batched", 0, 10_000, FORM_BATCHED, None),
+             ("reads_100_250bp_1M_pairs_30pct_unrelated", 1, 1_000_000, FORM_BATCHED, None),
+             ("250bp_vs_2_8kb_refs_200k_pairs", 4, 200_000, FORM_BATCHED, None),
+             ("uneven_200k_pairs_all_int32", 2, 200_000, FORM_BATCHED, 0)]
+    default_ceiling = limits().int16_ceiling
+    for name, cfg, n, form, ceiling in specs:
+        pp = workloads.generate(cfg, n=n)
+        tens = [torch.from_numpy(x).to(dev) for x in (pp.a_seq, pp.a_off, pp.a_len, pp.b_seq, pp.b_off, pp.b_len)]
+        o = torch.empty((pp.n, 5), dtype=torch.int32, device=dev)
+        cells = float(pp.cells())
+        dp = DevicePairs(*(t.data_ptr() for t in tens), n=pp.n, max_a_len=int(pp.a_len.max()),
+                         max_b_len=int(pp.b_len.max()), cells=cells, a_bytes=int((pp.a_off + pp.a_len).max()),
+                         b_bytes=int((pp.b_off + pp.b_len).max()))
+        drv.set_int16_ceiling(default_ceiling if ceiling is None else ceiling)
+        for _ in range(2):
+            drv.align_pairs_device(dp, o.data_ptr(), form=form)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fwd = []
+        for _ in range(3):
+            drv.align_pairs_device(dp, o.data_ptr(), form=form)
+            fwd.append(drv.last_timing()["fwd_ms"])
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / 3
+        t = drv.last_timing()
+        out[name] = {"gcups": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms, "pairs": pp.n, "cells": cells,
+                     "fwd_gcups": cells / (statistics.mean(fwd) * 1e-3) / 1e9,
+                     "int32_reruns": int(t["n_overflow16"]), "form": "plain" if form == FORM_PLAIN else "batched"}
+        del tens, o
+        torch.cuda.empty_cache()
+    drv.set_int16_ceiling(default_ceiling)
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -229,6 +277,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-paths", action="store_true", help="skip the per-workload path measurements")
     ap.add_argument("--workload", choices=["batch", "serving"], default="batch",
                     help="batch: the uneven-length batch (default); serving: latency under offered load")
     ap.add_argument("--slots", type=int, default=3, help="serving: micro-batches in flight")
@@ -369,8 +418,20 @@ def main() -> None:
     # the e2e results must equal the resident-input results
     assert np.array_equal(hout, out_dev.cpu().numpy()), "e2e results differ from device-resident results"
 
+    # ---- other paths of the scope: per-workload GCUPS, device-resident ----------------
+    paths = None
+    if rank == 0 and not args.no_paths:
+        paths = run_paths(drv, dev, torch, stream)
+
     # ---- roofline of the dominant kernel (the persistent forward kernel) -------------
     dpx_ops, sm_hz = probe_dpx_rate(local)
+    hbm_peak, hbm_basis = 6800.0, "fallback 6.8 TB/s"
+    mp = ROOT / "MEASURED_PEAKS.json"
+    if mp.exists():
+        try:
+            hbm_peak, hbm_basis = float(json.loads(mp.read_text())["hbm_gbs"]), "measured copy bandwidth"
+        except (KeyError, ValueError):
+            pass
     peak_gcups = dpx_ops * 2 / K_OPS_PER_CELL_PAIR / 1e9
     fwd_avg = statistics.mean(fwd_ms)
     achieved = cells_local / (fwd_avg * 1e-3) / 1e9
@@ -389,8 +450,8 @@ def main() -> None:
         "traffic": traffic, "kernel": "k_fwd_persist (batched forward pass)",
         "peak_basis": f"measured packed-int16 DPX add-max rate {dpx_ops / 1e12:.2f} T/s x 2 cells / "
                       f"{K_OPS_PER_CELL_PAIR} ops per packed cell pair",
-        "hbm": {"achieved": alg_bytes / (fwd_avg * 1e-3) / 1e9, "peak": 6761.6, "unit": "GB/s",
-                "frac": alg_bytes / (fwd_avg * 1e-3) / 1e9 / 6761.6},
+        "hbm": {"achieved": alg_bytes / (fwd_avg * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": alg_bytes / (fwd_avg * 1e-3) / 1e9 / hbm_peak, "peak_basis": hbm_basis},
     }
 
     cpu = None
@@ -414,8 +475,8 @@ def main() -> None:
                     "ms_per_step": e2e_s * 1e3},
             "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "paths": paths,
             "overflow16_pairs": int(last["n_overflow16"]), "rev_wavefront_pairs": int(last["n_rev_wide"]),
-            "sm_hz_probe": sm_hz,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -139,6 +139,10 @@ extern "C" int mhsw_probe_dpx_rate(int device, double *ops_per_s, double *sm_hz)
   const double ops = (double)blocks * threads * kIters * kChains * reps / 32.0;  // warp instructions
   const double secs = ms * 1e-3;
   *ops_per_s = ops * 32.0 / secs;  // lane-level packed instructions per second
-  *sm_hz = mean_cyc / (secs / reps);
+  // blocks run in waves when fewer than 8 fit on an SM: each block's cycles cover one wave
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dpx_probe, threads, 0);
+  const int waves = per_sm > 0 ? (blocks + sms * per_sm - 1) / (sms * per_sm) : 1;
+  *sm_hz = mean_cyc * waves / (secs / reps);
   return MHSW_OK;
 }
