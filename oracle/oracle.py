@@ -52,6 +52,7 @@ def oracle_lib() -> C.CDLL:
             build(with_reference=False)
         lib = C.CDLL(str(ORACLE_SO))
         _bind(lib, "sw_oracle_align_batch")
+        _bind(lib, "sw_oracle_align_batch7")
         lib.sw_oracle_align_codes.restype = C.c_int64
         lib.sw_oracle_align_codes.argtypes = [_P, C.c_int, _P, C.c_int, _P, C.c_int, C.c_int, _P]
         _ORACLE = lib
@@ -69,6 +70,7 @@ def ref_lib() -> C.CDLL:
             raise RuntimeError("reference SSW not built (oracle/_ref/libssw_ref.so)")
         lib = C.CDLL(str(REF_SO))
         _bind(lib, "ssw_ref_align_batch")
+        _bind(lib, "ssw_ref_align_batch7")
         lib.ssw_ref_align.restype = C.c_int
         lib.ssw_ref_align.argtypes = [C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_int, C.c_int, _P]
@@ -76,9 +78,9 @@ def ref_lib() -> C.CDLL:
     return _REF
 
 
-def _run(lib, fn, pairs, scoring, threads):
+def _run(lib, fn, pairs, scoring, threads, width=5):
     n = pairs.n
-    out = np.zeros((n, 5), dtype=np.int32)
+    out = np.zeros((n, width), dtype=np.int32)
     if n == 0:
         return out
     m, x, go, ge, amb = scoring
@@ -90,14 +92,20 @@ def _run(lib, fn, pairs, scoring, threads):
     return out
 
 
-def align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None) -> np.ndarray:
-    """Oracle results n x 5 (score, a_begin, a_end, b_begin, b_end); scoring =
+def align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, score2: bool = False) -> np.ndarray:
+    """Oracle results n x 5 (score, a_begin, a_end, b_begin, b_end), or n x 7 with score2
+    and a_end2 (SSW's second-best score, maskLen = max(len(A)/2, 15)); scoring =
     (match, mismatch, gap_open, gap_extend, ambiguity) as positive magnitudes."""
+    if score2:
+        return _run(oracle_lib(), "sw_oracle_align_batch7", pairs, scoring, threads or (os.cpu_count() or 1), 7)
     return _run(oracle_lib(), "sw_oracle_align_batch", pairs, scoring, threads or (os.cpu_count() or 1))
 
 
-def ref_align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None) -> np.ndarray:
-    """The reference SSW, called as klign calls it (src/klign.cpp:257)."""
+def ref_align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, score2: bool = False) -> np.ndarray:
+    """The reference SSW, called as klign calls it (src/klign.cpp:257); n x 7 with
+    sw_score_next_best and ref_end_next_best when score2."""
+    if score2:
+        return _run(ref_lib(), "ssw_ref_align_batch7", pairs, scoring, threads or (os.cpu_count() or 1), 7)
     return _run(ref_lib(), "ssw_ref_align_batch", pairs, scoring, threads or (os.cpu_count() or 1))
 
 

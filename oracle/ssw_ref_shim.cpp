@@ -53,6 +53,7 @@ struct RefBatch {
   int match, mismatch, gO, gE, amb;
   int32_t *out;
   int64_t next;
+  int width;  // 5: score and coordinates; 7: plus sw_score_next_best and ref_end_next_best
   pthread_mutex_t mu;
 };
 
@@ -77,22 +78,26 @@ static void *ref_worker(void *arg) {
       int mask_len = rl / 2 > 15 ? rl / 2 : 15;
       aln.Clear();
       aligner.Align(q.c_str(), bt->a_seqs + bt->a_off[p], rl, filter, &aln, mask_len);
-      int32_t *o = bt->out + 5 * p;
+      int32_t *o = bt->out + bt->width * p;
       o[0] = aln.sw_score;
       o[1] = aln.ref_begin;
       o[2] = aln.ref_end;
       o[3] = aln.query_begin;
       o[4] = aln.query_end;
+      if (bt->width == 7) {
+        o[5] = aln.sw_score_next_best;
+        o[6] = aln.ref_end_next_best;
+      }
     }
   }
   return nullptr;
 }
 
-// Same layout as sw_oracle_align_batch: out[5p..5p+4] = score, a_begin, a_end, b_begin, b_end.
-int ssw_ref_align_batch(const char *a_seqs, const int64_t *a_off, const int32_t *a_len, const char *b_seqs,
-                        const int64_t *b_off, const int32_t *b_len, int64_t n, int match, int mismatch, int gap_open,
-                        int gap_extend, int ambiguity, int nthreads, int32_t *out) {
+static int ref_batch_run(const char *a_seqs, const int64_t *a_off, const int32_t *a_len, const char *b_seqs,
+                         const int64_t *b_off, const int32_t *b_len, int64_t n, int match, int mismatch, int gap_open,
+                         int gap_extend, int ambiguity, int nthreads, int32_t *out, int width) {
   RefBatch bt;
+  bt.width = width;
   bt.a_seqs = a_seqs;
   bt.b_seqs = b_seqs;
   bt.a_off = a_off;
@@ -115,6 +120,22 @@ int ssw_ref_align_batch(const char *a_seqs, const int64_t *a_off, const int32_t 
   for (int t = 1; t < nthreads; t++) pthread_join(th[t], nullptr);
   pthread_mutex_destroy(&bt.mu);
   return 0;
+}
+
+// Same layout as sw_oracle_align_batch: out[5p..5p+4] = score, a_begin, a_end, b_begin, b_end.
+int ssw_ref_align_batch(const char *a_seqs, const int64_t *a_off, const int32_t *a_len, const char *b_seqs,
+                        const int64_t *b_off, const int32_t *b_len, int64_t n, int match, int mismatch, int gap_open,
+                        int gap_extend, int ambiguity, int nthreads, int32_t *out) {
+  return ref_batch_run(a_seqs, a_off, a_len, b_seqs, b_off, b_len, n, match, mismatch, gap_open, gap_extend, ambiguity,
+                       nthreads, out, 5);
+}
+
+// As sw_oracle_align_batch7: out[7p..7p+6] adds sw_score_next_best and ref_end_next_best.
+int ssw_ref_align_batch7(const char *a_seqs, const int64_t *a_off, const int32_t *a_len, const char *b_seqs,
+                         const int64_t *b_off, const int32_t *b_len, int64_t n, int match, int mismatch, int gap_open,
+                         int gap_extend, int ambiguity, int nthreads, int32_t *out) {
+  return ref_batch_run(a_seqs, a_off, a_len, b_seqs, b_off, b_len, n, match, mismatch, gap_open, gap_extend, ambiguity,
+                       nthreads, out, 7);
 }
 
 }  // extern "C"

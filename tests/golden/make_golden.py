@@ -14,6 +14,9 @@ $MHSW_REFERENCE) on x86_64; the GPU machine needs only the committed JSON files.
   ssw_reference_samples.json
       Seeded sample pairs of the measured workloads and hand-made edge cases with the
       reference SSW's (score, a_begin, a_end, b_begin, b_end) under those four scorings.
+  Both files also record, per scoring, the reference's second-best score and its row
+  ("reference_next_best": sw_score_next_best, ref_end_next_best) for maskLen =
+  max(len(A)/2, 15) as klign passes it.
 """
 from __future__ import annotations
 
@@ -108,9 +111,10 @@ def main() -> None:
     # A = SSW ref = the test's ref; B = SSW query = the test's query (Align(query, ref))
     pairs = Pairs.from_lists([c["ref"] for c in cases], [c["query"] for c in cases])
     for name, sc in SCORINGS.items():
-        out = oracle.ref_align_batch(pairs, sc, 1)
+        out = oracle.ref_align_batch(pairs, sc, 1, score2=True)
         for c, o in zip(cases, out.tolist()):
-            c.setdefault("reference", {})[name] = o
+            c.setdefault("reference", {})[name] = o[:5]
+            c.setdefault("reference_next_best", {})[name] = o[5:7]
     for c, a in zip(cases, adept):
         assert (c["query"], c["ref"]) == (a["query"], a["ref"])
         c["adept_expect"] = {"qbegin": a["qstart"], "qend": a["qend"], "rbegin": a["rstart"], "rend": a["rend"]}
@@ -134,11 +138,12 @@ def main() -> None:
     ]
     samples += edge
     sp = Pairs.from_lists([s[1] for s in samples], [s[2] for s in samples])
-    rec = [{"set": s[0], "a": s[1], "b": s[2], "reference": {}} for s in samples]
+    rec = [{"set": s[0], "a": s[1], "b": s[2], "reference": {}, "reference_next_best": {}} for s in samples]
     for name, sc in SCORINGS.items():
-        out = oracle.ref_align_batch(sp, sc, 1)
+        out = oracle.ref_align_batch(sp, sc, 1, score2=True)
         for r, o in zip(rec, out.tolist()):
-            r["reference"][name] = o
+            r["reference"][name] = o[:5]
+            r["reference_next_best"][name] = o[5:7]
     (HERE / "ssw_reference_samples.json").write_text(json.dumps(
         {"source": "reference SSW (src/ssw/ssw.cpp + ssw_core.cpp) called as klign calls it (src/klign.cpp:257)",
          "orientation": "a = SSW ref (klign: the read), b = SSW query (klign: the contig window)",

@@ -107,3 +107,34 @@ def test_generated_workloads_vs_live_reference():
         got = oracle.align_batch(p)
         want = oracle.ref_align_batch(p)
         assert np.array_equal(got, want), cfg
+
+
+@pytest.mark.parametrize("scoring", list(SAMPLES["scorings"]))
+def test_second_best_vs_recorded_reference(scoring):
+    """score2 / a_end2 (SSW's sw_score_next_best / ref_end_next_best, maskLen = max(len/2, 15))
+    against the recorded reference outputs; the first five columns are unchanged."""
+    recs = SAMPLES["pairs"]
+    pairs = Pairs.from_lists([r["a"] for r in recs], [r["b"] for r in recs])
+    out = oracle.align_batch(pairs, tuple(SAMPLES["scorings"][scoring]), score2=True)
+    want = np.array([r["reference"][scoring] + r["reference_next_best"][scoring] for r in recs], dtype=np.int32)
+    bad = np.nonzero((out != want).any(axis=1))[0]
+    assert len(bad) == 0, [(recs[i]["set"], out[i].tolist(), want[i].tolist()) for i in bad[:3]]
+    cases, kp = _kat_pairs()
+    kout = oracle.align_batch(kp, tuple(KAT["scorings"][scoring]), score2=True)
+    kwant = np.array([c["reference"][scoring] + c["reference_next_best"][scoring] for c in cases], dtype=np.int32)
+    assert np.array_equal(kout, kwant)
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference SSW not built (needs the reference checkout)")
+def test_second_best_vs_live_reference():
+    """Including the word path (scores >= 255 - bias with match 2) and SSW's zero-score
+    query padding, which reaches into maxColumn."""
+    from mhm2_staging_gb300 import workloads
+
+    for cfg, n in ((0, 1500), (1, 3000), (2, 1500), (4, 120)):
+        p = workloads.generate(cfg, n=n, first=321)
+        for sc in [(1, 3, 5, 2, 2), (2, 2, 3, 1, 2), (2, 4, 4, 2, 1)]:
+            got = oracle.align_batch(p, sc, score2=True)
+            want = oracle.ref_align_batch(p, sc, score2=True)
+            bad = np.nonzero((got != want).any(axis=1))[0]
+            assert len(bad) == 0, (cfg, sc, got[bad[:2]].tolist(), want[bad[:2]].tolist())
