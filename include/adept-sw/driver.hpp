@@ -131,6 +131,16 @@ class GPUDriver {
     detail::check(mhsw_driver_set_orientation(drv_, orientation), drv_, "set_orientation");
   }
   void set_form(int form) { detail::check(mhsw_driver_set_form(drv_, form), drv_, "set_form"); }
+  // Score2 mode: also compute SSW's second-best score per pair (klign's aln.score2, which
+  // its GPU path otherwise sets to 0, src/klign.cpp:377-378).
+  void set_score2(bool on) { detail::check(mhsw_driver_set_score2(drv_, on ? 1 : 0), drv_, "set_score2"); }
+  // After run_kernel_forwards in score2 mode: the batch's second-best scores (driver-owned,
+  // valid until the next run_kernel_*); nullptr when the mode is off.
+  const int32_t *get_score2() {
+    mhsw_aln_results r;
+    detail::check(mhsw_get_aln_results(drv_, &r), drv_, "get_aln_results");
+    return r.score2_32;
+  }
 
   void run_kernel_forwards(std::vector<std::string> &reads, std::vector<std::string> &contigs, unsigned maxReadSize,
                            unsigned maxContigSize) {

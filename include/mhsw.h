@@ -61,6 +61,10 @@ typedef struct {
   int16_t *ref_begin, *query_begin, *ref_end, *query_end, *top_scores;
   int32_t *ref_begin32, *query_begin32, *ref_end32, *query_end32, *top_scores32;
   int32_t n;
+  /* score2 mode only (else NULL; see mhsw_driver_set_score2): SSW's second-best score
+   * (sw_score_next_best) and its A row (ref_end_next_best: the read row in klign's
+   * orientation), filled by run_kernel_forwards. */
+  int32_t *score2_32, *a_end2_32;
 } mhsw_aln_results;
 
 /* Device-timed figures of the last mhsw_align_pairs / run_kernel_* call. */
@@ -146,6 +150,17 @@ int mhsw_driver_set_form(mhsw_driver *drv, int form);
 int mhsw_driver_set_int16_ceiling(mhsw_driver *drv, int ceiling);
 /* The CUDA stream (cudaStream_t) the handle launches on. */
 int mhsw_driver_stream(mhsw_driver *drv, void **stream);
+/* Score2 mode (default off).  klign's CPU path keeps SSW's second-best score
+ * (aln.score2 = sw_score_next_best, src/klign.cpp:267); the reference GPU driver has no
+ * such output and klign writes 0 (src/klign.cpp:377-378).  With the mode on, the forward
+ * pass also computes it exactly as SSW does (ssw_core.cpp:513-536, :825-847, :1154-1160,
+ * maskLen = max(len(A)/2, 15) as klign passes it, SSW's zero-score query padding
+ * included); it costs one extra add-max per cell pair.  Results: mhsw_last_score2 and,
+ * for the drop-in protocol, mhsw_aln_results.score2_32 / a_end2_32. */
+int mhsw_driver_set_score2(mhsw_driver *drv, int on);
+/* Second-best scores of the last batch aligned in score2 mode: score2[i] and its A row
+ * a_end2[i] (0 and 0 when no row qualifies), host or device pointers as host_io says. */
+int mhsw_last_score2(mhsw_driver *drv, int32_t *score2, int32_t *a_end2, int host_io);
 
 /* GPUDriver::run_kernel_forwards (driver.cpp:281-375): copies the batch, launches
  * the forward pass and the copy of the end coordinates and scores; returns without

@@ -68,7 +68,7 @@ __global__ void k_split(const uint32_t *__restrict__ keys, int64_t n, int *split
 // Persistent forward kernel over one range of the sorted pair order: 8-lane groups for
 // the short-read buckets (items [0, split)), 16-lane groups for the rest ([split, n)).
 // A group claims its next pair from the range's atomic counter.
-template <int G>
+template <int G, bool S2 = false>
 __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, Scoring sc,
                                                      const uint32_t *__restrict__ keys,
                                                      const uint32_t *__restrict__ order, int64_t n, int *queue,
@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, S
   const int grp = threadIdx.x / G;
   const int lane = threadIdx.x % G;
   const unsigned gmask = group_mask_b(G);
-  constexpr size_t kProf = kShort ? group_prof16_bytes<10, G>() : group_prof16_bytes<8, G>();
+  constexpr int kC = S2 ? kCode16Zero + 1 : kCodeN + 1;
+  constexpr size_t kProf = kShort ? group_prof16_bytes<10, G, kC>() : group_prof16_bytes<8, G, kC>();
   unsigned char *gbase = smem + (size_t)grp * kProf;  // keyed engine: profile table only
   GroupSmem gs;
   gs.prof = reinterpret_cast<uint32_t *>(gbase);
@@ -115,7 +116,8 @@ __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, S
       }
       continue;
     }
-    const bool too_long = (N > kMaxB) || (bucket == kBucketStrip && (bnd == nullptr || N > scratch_stride));
+    const int NP = S2 ? ssw_pad16(N) : N;
+    const bool too_long = (N > kMaxB) || (bucket == kBucketStrip && (bnd == nullptr || NP > scratch_stride));
     if (M <= 0 || N <= 0 || too_long) {
       if (lane == 0) {
         rs.score[p] = 0;
@@ -128,20 +130,25 @@ __global__ void __launch_bounds__(256) k_fwd_persist(PairSet ps, ResultSet rs, S
     SeqView A{ps.a_code + ps.a_off[p], 1, M};
     SeqView B{ps.b_code + ps.b_off[p], 1, N};
     SweepOut so;
+    RowMaxOut rmo{nullptr, 0};
+    if constexpr (S2) rmo = RowMaxOut{ps.rowmax16 + ps.a_off[p], NP};
     if constexpr (kShort) {
       switch (bucket) {
-        case 0: sweep16<4, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-        case 1: sweep16<6, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-        case 2: sweep16<8, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
-        default: sweep16<10, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so); break;
+        case 0: sweep16<4, G, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, so, rmo); break;
+        case 1: sweep16<6, G, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, so, rmo); break;
+        case 2: sweep16<8, G, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, so, rmo); break;
+        default: sweep16<10, G, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, so, rmo); break;
       }
     } else {
-      if (bucket == 4) sweep16<6, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so);
-      else sweep16<8, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so);
+      if (bucket == 4) sweep16<6, G, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, so, rmo);
+      else sweep16<8, G, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, so, rmo);
     }
     if (lane == 0) {
       const int S = key_value(so.key);
-      if (so.overflow) {
+      // score2 mode: the word path's padding differs from the one swept here; the int32
+      // pass recomputes those row maxima
+      const bool word_redo = S2 && S + ssw_bias(sc) >= 255 && ssw_pad8(N) != NP;
+      if (so.overflow || word_redo) {
         rs.flag[p] = kFlagOverflow16;
         const int slot = atomicAdd(wl.ovf_count, 1);
         if (slot < wl.cap) wl.ovf[slot] = p;
@@ -220,12 +227,14 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     bs.err = "B longer than the kernel limit";
     return 1;
   }
-  auto kshort = k_fwd_persist<kGKShort>;
-  auto klong = k_fwd_persist<kGKLong>;
-  const size_t prof_short = group_prof16_bytes<10, kGKShort>();
-  const size_t prof_long = group_prof16_bytes<8, kGKLong>();
+  const bool s2 = ps.rowmax16 != nullptr;
+  auto kshort = s2 ? k_fwd_persist<kGKShort, true> : k_fwd_persist<kGKShort, false>;
+  auto klong = s2 ? k_fwd_persist<kGKLong, true> : k_fwd_persist<kGKLong, false>;
+  const size_t prof_short = s2 ? group_prof16_bytes<10, kGKShort, kCode16Zero + 1>() : group_prof16_bytes<10, kGKShort>();
+  const size_t prof_long = s2 ? group_prof16_bytes<8, kGKLong, kCode16Zero + 1>() : group_prof16_bytes<8, kGKLong>();
   const int pad = 2 * kGKLong;
-  const int bcap = ((pad + std::max(max_b, 1) + 2 * kGKLong) + 15) / 16 * 16;  // strip scratch stride
+  // strip scratch stride: B, the lane skew and score2 mode's zero-score padding (< 16)
+  const int bcap = ((pad + std::max(max_b, 1) + 16 + 2 * kGKLong) + 15) / 16 * 16;
 
   // keys + sort (the order is reused by every tuning trial)
   {

@@ -106,6 +106,11 @@ struct mhsw_driver {
   DBuf<unsigned char> outv;  // 5 x int16 + 5 x int32 arrays
   DBuf<int32_t> out5;
   mhsw::BatchState batch;     // batched-form work buffers
+  // score2 mode: SSW's second-best score per pair (row maxima arenas, results)
+  bool score2 = false;
+  int64_t score2_n = -1;  // pairs of the last batch whose second-best scores are in r_score2
+  DBuf<int32_t> rowmax16, rowmax8, r_score2, r_aend2;
+  HBuf<int32_t> h_score2;  // drop-in protocol: score2 then a_end2, n each
   mhsw::Forks forks;          // side streams for launches that overlap on the device
 
   // CUDA graph of a device-resident batch: captured the second time the same batch
@@ -114,7 +119,7 @@ struct mhsw_driver {
     const void *ptr[7];
     int64_t n, a_bytes, b_bytes;
     int32_t max_a, max_b;
-    int form, ceiling, match, mismatch, gap_open, gap_extend, ambiguity;
+    int form, ceiling, match, mismatch, gap_open, gap_extend, ambiguity, score2;
     bool operator==(const GraphKey &o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
   };
   GraphKey gkey{};
@@ -181,6 +186,11 @@ struct mhsw_driver {
     outv.release();
     out5.release();
     batch.release();
+    rowmax16.release();
+    rowmax8.release();
+    r_score2.release();
+    r_aend2.release();
+    h_score2.release();
     h_a.release();
     h_b.release();
     h_aoff.release();
@@ -239,7 +249,25 @@ mhsw::ResultSet result_set(mhsw_driver *d) {
   rs.a_beg = d->r_abeg.p;
   rs.b_beg = d->r_bbeg.p;
   rs.flag = d->r_flag.p;
+  if (d->score2) {
+    rs.score2 = d->r_score2.p;
+    rs.a_end2 = d->r_aend2.p;
+  }
   return rs;
+}
+
+// Score2 mode: row-maxima arenas at the A offsets and the result arrays; the pair set
+// then selects the forward kernels' score2 variants.
+int attach_score2(mhsw_driver *d, mhsw::PairSet *ps, int64_t n, int64_t a_bytes) {
+  ps->rowmax16 = ps->rowmax8 = nullptr;
+  if (!d->score2 || n <= 0) return MHSW_OK;
+  MHSW_CK(d->rowmax16.reserve((size_t)a_bytes + 16), "cudaMalloc row maxima");
+  MHSW_CK(d->rowmax8.reserve((size_t)a_bytes + 16), "cudaMalloc row maxima");
+  MHSW_CK(d->r_score2.reserve((size_t)n + 1), "cudaMalloc results");
+  MHSW_CK(d->r_aend2.reserve((size_t)n + 1), "cudaMalloc results");
+  ps->rowmax16 = d->rowmax16.p;
+  ps->rowmax8 = d->rowmax8.p;
+  return MHSW_OK;
 }
 
 mhsw::WorkLists work_lists(mhsw_driver *d, int64_t n) {
@@ -288,7 +316,8 @@ int ceiling_for(mhsw_driver *d) {
 
 int run_forward(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, bool persistent_grid) {
   mhsw::FwdConfig c16, c32;
-  cudaError_t e = mhsw::plan_forward(d->device, max_a, max_b, false, &c16, mhsw::keyed_scoring(d->sc));
+  cudaError_t e = mhsw::plan_forward(d->device, max_a, max_b, false, &c16, mhsw::keyed_scoring(d->sc),
+                                     ps.rowmax16 != nullptr);
   if (e != cudaSuccess) return d->fail(MHSW_ERR_LIMIT, "B length %d exceeds the kernel limit %d", max_b, mhsw::kMaxB);
   e = mhsw::plan_forward(d->device, max_a, max_b, true, &c32);
   if (e != cudaSuccess) return d->fail(MHSW_ERR_LIMIT, "B length %d exceeds the kernel limit %d", max_b, mhsw::kMaxB);
@@ -312,7 +341,20 @@ int run_forward(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, b
 }
 
 // Forward pass in either form; lists are reset first so both passes see fresh counters.
+int forward_passes(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, int form);
+
+// Forward pass, then (score2 mode) the second-best scores from the row maxima it wrote.
 int forward_any(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, int form) {
+  d->score2_n = -1;
+  int rc = forward_passes(d, ps, max_a, max_b, form);
+  if (rc || !ps.rowmax16) return rc;
+  MHSW_CK(mhsw::launch_score2(ps, result_set(d), d->sc, d->st), "score2 launch");
+  d->launches += 1;
+  d->score2_n = ps.n;
+  return MHSW_OK;
+}
+
+int forward_passes(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, int form) {
   // The batched form runs the keyed int16 engine; scorings it cannot hold (a mismatch or
   // ambiguity penalty above the gap-open penalty) use the plain form.
   d->fwd_order = nullptr;
@@ -326,7 +368,7 @@ int forward_any(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b, i
   d->fwd_order = d->batch.idx_out;
   // int32 pass over the pairs the int16 engine could not hold
   mhsw::FwdConfig c16, c32;
-  if (mhsw::plan_forward(d->device, max_a, max_b, false, &c16) != cudaSuccess ||
+  if (mhsw::plan_forward(d->device, max_a, max_b, false, &c16, false, ps.rowmax16 != nullptr) != cudaSuccess ||
       mhsw::plan_forward(d->device, max_a, max_b, true, &c32) != cudaSuccess)
     return d->fail(MHSW_ERR_LIMIT, "B length %d exceeds the kernel limit %d", max_b, mhsw::kMaxB);
   size_t sb = 0;
@@ -687,10 +729,19 @@ int mhsw_run_kernel_forwards(mhsw_driver *d, const char *const *reads, const int
     rc = translate_batch(d, &ps, d->a_bytes, d->b_bytes);
     if (rc) return rc;
   }
+  rc = attach_score2(d, &ps, n, d->a_bytes);
+  if (rc) return rc;
   MHSW_CK(cudaEventRecord(d->ev_t[1], d->st), "event");
   if (n > 0) {
     rc = forward_any(d, ps, d->max_a, d->max_b, d->form);
     if (rc) return rc;
+    if (ps.rowmax16) {
+      MHSW_CK(d->h_score2.reserve(2 * (size_t)n), "cudaMallocHost");
+      MHSW_CK(cudaMemcpyAsync(d->h_score2.p, d->r_score2.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, d->st),
+              "D2H");
+      MHSW_CK(cudaMemcpyAsync(d->h_score2.p + n, d->r_aend2.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, d->st),
+              "D2H");
+    }
   }
   MHSW_CK(cudaEventRecord(d->ev_t[2], d->st), "event");
   mhsw::OutViews dv, hv;
@@ -824,6 +875,9 @@ int mhsw_get_aln_results(mhsw_driver *d, mhsw_aln_results *out) {
   out->query_begin32 = w + 3 * n;
   out->query_end32 = w + 4 * n;
   out->n = (int32_t)d->n_batch;
+  const bool s2 = d->score2 && d->h_score2.p && d->n_batch > 0;
+  out->score2_32 = s2 ? d->h_score2.p : nullptr;
+  out->a_end2_32 = s2 ? d->h_score2.p + d->n_batch : nullptr;
   return MHSW_OK;
 }
 
@@ -926,6 +980,8 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
     MHSW_CK(d->h_counts.reserve(4), "cudaMallocHost");
     if (host_io) MHSW_CK(d->out5.reserve((size_t)n * 5), "cudaMalloc out5");
   }
+  rc = attach_score2(d, &ps, n, ta);
+  if (rc) return rc;
   // Everything from translation to the result copy, on the handle's stream.
   // Phase events recorded inside a capture become external event nodes, so a replayed
   // graph still records them and the phase timings stay available.
@@ -981,6 +1037,7 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
     key.gap_open = d->sc.gap_open;
     key.gap_extend = d->sc.gap_extend;
     key.ambiguity = d->sc.ambiguity;
+    key.score2 = d->score2 ? 1 : 0;
   }
   const bool same = hinted && d->use_graphs && n > 0 && d->gkey_seen && key == d->gkey;
   if (same && d->gexec) {
@@ -1051,6 +1108,28 @@ int mhsw_last_timing(mhsw_driver *d, mhsw_timing *out) {
   if (!d || !out) return MHSW_ERR_ARG;
   std::lock_guard<std::mutex> lk(d->mu);
   *out = d->timing;
+  return MHSW_OK;
+}
+
+int mhsw_driver_set_score2(mhsw_driver *d, int on) {
+  if (!d) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  d->score2 = on != 0;
+  return MHSW_OK;
+}
+
+int mhsw_last_score2(mhsw_driver *d, int32_t *score2, int32_t *a_end2, int host_io) {
+  int rc = ready(d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(d->mu);
+  const int64_t n = d->score2_n;
+  if (n < 0 || !d->r_score2.p) return d->fail(MHSW_ERR_STATE, "score2 mode was off for the last batch");
+  if (n > 0 && (!score2 || !a_end2)) return d->fail(MHSW_ERR_ARG, "NULL output");
+  if (n <= 0) return MHSW_OK;
+  const cudaMemcpyKind k = host_io ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  MHSW_CK(cudaMemcpyAsync(score2, d->r_score2.p, sizeof(int32_t) * n, k, d->st), "copy score2");
+  MHSW_CK(cudaMemcpyAsync(a_end2, d->r_aend2.p, sizeof(int32_t) * n, k, d->st), "copy score2");
+  MHSW_CK(cudaStreamSynchronize(d->st), "sync");
   return MHSW_OK;
 }
 

@@ -53,6 +53,7 @@ static __constant__ uint8_t c_code[256] = {
 
 __host__ __device__ inline int sub_score(int a, int b, const Scoring &s, int big) {
   if (a == kCodePad || b == kCodePad) return -big;
+  if (b == kCodeZeroPad) return 0;
   if (a == kCodeN || b == kCodeN) return -s.ambiguity;
   return a == b ? s.match : -s.mismatch;
 }
@@ -256,9 +257,19 @@ struct SweepOut {
 //                A fits one strip)
 //   ceiling    : int16 overflow ceiling (values above it flag overflow)
 // ---------------------------------------------------------------------------------
-template <class VT, int K, int G>
+// Score2 mode of the generic engine: the sweep covers P16 columns ([N, P16) score 0, SSW's
+// byte-path query padding) and keeps two maxima per A row, over columns [0, P16) and over
+// [0, P8) (the word path pads to a multiple of 8); both are written, and the second-best
+// score reads the one of the path SSW took.
+struct RowMaxOut2 {
+  int32_t *rowmax16, *rowmax8;
+  int P16, P8;
+};
+
+template <class VT, int K, int G, bool S2 = false>
 __device__ void sweep_pair(const SeqView &A, const SeqView &B, const Scoring &sc, const GroupSmem &gs, int lane,
-                           unsigned gmask, typename VT::Pay *bnd, int ceiling, SweepOut &out) {
+                           unsigned gmask, typename VT::Pay *bnd, int ceiling, SweepOut &out,
+                           const RowMaxOut2 &rm2 = RowMaxOut2{nullptr, nullptr, 0, 0}) {
   const int lane_in_block = lane;  // table column: lane within the group
   using T = typename VT::T;
   using Pay = typename VT::Pay;
@@ -267,18 +278,20 @@ __device__ void sweep_pair(const SeqView &A, const SeqView &B, const Scoring &sc
   const T NGO = VT::splat(-sc.gap_open);
   const T NGE = VT::splat(-sc.gap_extend);
 
-  // B codes into shared memory: bcodes[pad + j] for j in [-pad, N + 2G); PAD outside [0, N).
-  const int fill = gs.pad + N + 2 * G < gs.bcap ? gs.pad + N + 2 * G : gs.bcap;
+  const int NP = S2 ? rm2.P16 : N;  // columns swept
+  // B codes into shared memory: bcodes[pad + j] for j in [-pad, NP + 2G); PAD outside
+  // [0, N) except the zero-score columns [N, NP) of score2 mode.
+  const int fill = gs.pad + NP + 2 * G < gs.bcap ? gs.pad + NP + 2 * G : gs.bcap;
   for (int x = lane; x < fill; x += G) {
     int j = x - gs.pad;
-    gs.bcodes[x] = (uint8_t)B.code(j);
+    gs.bcodes[x] = (uint8_t)((S2 && j >= N && j < NP) ? kCodeZeroPad : B.code(j));
   }
   __syncwarp(gmask);
 
   unsigned long long best = 0ull;
   int overflow = 0;
   const int nstrips = (M + RS - 1) / RS;
-  const int T_end = N + 2 * G - 1;  // steps per strip
+  const int T_end = NP + 2 * G - 1;  // steps per strip
 
   for (int s = 0; s < nstrips; s++) {
     const int row0 = s * RS + lane * 2 * K;
@@ -296,6 +309,7 @@ __device__ void sweep_pair(const SeqView &A, const SeqView &B, const Scoring &sc
 
     T H[K], F[K], V[K], Pprev[K];
     int Jlo[K], Jhi[K];
+    int R16lo[K], R16hi[K], R8lo[K], R8hi[K];  // score2 mode: row maxima over valid columns
 #pragma unroll
     for (int k = 0; k < K; k++) {
       H[k] = VT::splat(0);
@@ -303,6 +317,7 @@ __device__ void sweep_pair(const SeqView &A, const SeqView &B, const Scoring &sc
       V[k] = VT::splat(0);
       Jlo[k] = -1;
       Jhi[k] = -1;
+      R16lo[k] = R16hi[k] = R8lo[k] = R8hi[k] = 0;
     }
     load_profile<VT, K>(gs.prof, gs.prof_lanes, lane_in_block, kCodePad, Pprev);
     T Hlast = VT::splat(0);
@@ -323,12 +338,14 @@ __device__ void sweep_pair(const SeqView &A, const SeqView &B, const Scoring &sc
       if (lane == 0) {
         // Top boundary: row -1 for the first strip, else the previous strip's last row.
         z = ztop0;
-        if (!first_strip && j < N) z = bnd[j];
+        if (!first_strip && j < NP) z = bnd[j];
       }
       T Ev = VT::etop(z, Ecout);
       T Htop = VT::htop(z, Hlast);
       T Hd = HtopPrev;
       HtopPrev = Htop;
+      const bool ok16l = (unsigned)j < (unsigned)rm2.P16, ok16h = (unsigned)(j - 1) < (unsigned)rm2.P16;
+      const bool ok8l = (unsigned)j < (unsigned)rm2.P8, ok8h = (unsigned)(j - 1) < (unsigned)rm2.P8;
 
 #pragma unroll
       for (int k = 0; k < K; k++) {
@@ -348,6 +365,12 @@ __device__ void sweep_pair(const SeqView &A, const SeqView &B, const Scoring &sc
           Jlo[k] = hl > vl ? t : Jlo[k];
           Jhi[k] = hh > vh ? t : Jhi[k];
           V[k] = VT::max_relu(V[k], Hn);
+          if constexpr (S2) {
+            R16lo[k] = ok16l && hl > R16lo[k] ? hl : R16lo[k];
+            R16hi[k] = ok16h && hh > R16hi[k] ? hh : R16hi[k];
+            R8lo[k] = ok8l && hl > R8lo[k] ? hl : R8lo[k];
+            R8hi[k] = ok8h && hh > R8hi[k] ? hh : R8hi[k];
+          }
         }
         Pprev[k] = Pcur[k];
       }
@@ -356,7 +379,22 @@ __device__ void sweep_pair(const SeqView &A, const SeqView &B, const Scoring &sc
       Ecout = Ev;
       if (!last_strip && lane == G - 1) {
         const int jh = t - 2 * lane - 1;  // hi-half column of the last lane
-        if (jh >= 0 && jh < N) bnd[jh] = Zout;
+        if (jh >= 0 && jh < NP) bnd[jh] = Zout;
+      }
+    }
+
+    if constexpr (S2) {
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        const int rl = row0 + k, rh = row0 + K + k;
+        if (rl < M) {
+          rm2.rowmax16[rl] = R16lo[k];
+          rm2.rowmax8[rl] = R8lo[k];
+        }
+        if (rh < M) {
+          rm2.rowmax16[rh] = R16hi[k];
+          rm2.rowmax8[rh] = R8hi[k];
+        }
       }
     }
 

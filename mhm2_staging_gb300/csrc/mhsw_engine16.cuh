@@ -31,6 +31,14 @@
 //     loop is unrolled by two so the two word sets alternate registers).
 //  4. B codes are read from global memory (prefetched a step ahead) instead of being
 //     staged in shared memory, so a group's shared memory is its profile table only.
+//
+// Score2 mode (S2) also produces what SSW's second-best score is computed from
+// (ssw_core.cpp:489, :513-536): each A row's maximum of H, over B extended to P columns
+// by zero-scoring positions -- SSW pads its striped query to a multiple of 16 (byte
+// path) with positions that score 0 (qP_byte, ssw_core.cpp:191), and those reach its
+// per-row maxima.  The extra columns lie right of the real ones, so score and end are
+// unchanged.  The profile table then has a sixth code (zero score), and each row keeps a
+// running maximum over the valid columns (one DPX add-max per row and step).
 #pragma once
 #include "mhsw_engine.cuh"
 
@@ -48,10 +56,12 @@ __host__ __device__ constexpr int keyed_k_for_rows(int rows) {
 }
 __host__ __device__ constexpr int keyed_cap(int K) { return K <= 8 ? (1 << 12) - 64 : (1 << 11) - 64; }
 
-template <int K>
+constexpr int kCode16Zero = 5;  // score2 mode: SSW's zero-scoring query padding
+
+template <int K, int CODES = kCodeN + 1>
 struct Prof16 {
   static_assert(K % 2 == 0, "row pairs per lane must be even");
-  static constexpr int kCodes = kCodeN + 1;   // B codes A, C, G, T, N (outside B reads as N)
+  static constexpr int kCodes = CODES;        // B codes A, C, G, T, N (outside B reads as N) [, zero]
   static constexpr int kQ = K / 4;            // full vectors of low words (and of high words)
   static constexpr bool kRem = (K % 4) != 0;  // one vector: low K-2, K-1, high K-2, K-1
   static constexpr int kNV = 2 * kQ + (kRem ? 1 : 0);  // 128-bit vectors per (code, lane)
@@ -63,10 +73,17 @@ struct Prof16 {
   __host__ __device__ static constexpr int hi_elem(int w) { return w < 4 * kQ ? w % 4 : 2 + w - 4 * kQ; }
 };
 
-template <int KMAX, int G>
+template <int KMAX, int G, int CODES = kCodeN + 1>
 __host__ __device__ constexpr size_t group_prof16_bytes() {
-  return Prof16<KMAX>::bytes(G);
+  return Prof16<KMAX, CODES>::bytes(G);
 }
+
+// Where score2 mode writes the row maxima (rowmax[row] for the pair's A rows) and the
+// number of B columns it sweeps (P >= N; columns [N, P) score 0).
+struct RowMaxOut {
+  int32_t *rowmax;
+  int P;
+};
 
 __device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) {
   uint32_t r;
@@ -92,15 +109,17 @@ struct KeyBits {
   static constexpr int kCap = (1 << (15 - kBits)) - 64;  // largest score a key holds, with margin
 };
 
-template <int K, int G>
+template <int K, int G, bool S2 = false>
 struct Step16 {
-  using L = Prof16<K>;
+  using L = Prof16<K, S2 ? kCode16Zero + 1 : kCodeN + 1>;
   static constexpr uint32_t kKeyMask = KeyBits<K>::kMask;
+  // S2: Rm[k] keeps each row's running maximum over valid columns; vmask is 0 in a half
+  // whose column is valid at this step and -16384 otherwise (an add-max then ignores it).
   __device__ static __forceinline__ void run(int t, uint32_t z, const uint32_t (&Wlo)[K],
                                              const uint32_t (&Phi)[K], uint32_t (&H)[K], uint32_t (&F)[K],
                                              uint32_t &Hlast, uint32_t &Ecout, uint32_t &HtopPrev, uint32_t &Zout,
                                              uint32_t &Kl, uint32_t &Jp, uint32_t NGE, uint32_t NGO, uint32_t one,
-                                             uint32_t eight) {
+                                             uint32_t eight, uint32_t (&Rm)[K], uint32_t vmask) {
     uint32_t Ev = __byte_perm(z, Ecout, 0x5432);  // lo: from the left lane, hi: own lo half
     const uint32_t Htop = __byte_perm(z, Hlast, 0x5410);
     uint32_t Hd = HtopPrev;
@@ -118,6 +137,7 @@ struct Step16 {
       Hd = H[k];
       H[k] = Hn;
       key[k] = mad_u32(Hn, eight, (uint32_t)(kKeyMask - k) * 0x00010001u);
+      if constexpr (S2) Rm[k] = __viaddmax_s16x2(Hn, vmask, Rm[k]);
     }
     // running key per half (keys are non-negative int16): K/2 three-way maxima
     uint32_t Kn = Kl;
@@ -163,11 +183,11 @@ struct Step16 {
 // Forward sweep of one pair with the keyed engine.  B is read directly from its code
 // array in global memory (one byte per lane per step, prefetched a step ahead); the
 // shared memory of the group holds only the profile table.  A must be a forward view.
-template <int K, int G, bool MULTI>
+template <int K, int G, bool MULTI, bool S2 = false>
 __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &sc, const GroupSmem &gs, int lane,
-                             unsigned gmask, V16::Pay *bnd, int ceiling, SweepOut &out) {
-  using L = Prof16<K>;
-  using ST = Step16<K, G>;
+                             unsigned gmask, V16::Pay *bnd, int ceiling, SweepOut &out, const RowMaxOut &rmo) {
+  using ST = Step16<K, G, S2>;
+  using L = typename ST::L;
   constexpr int RS = 2 * K * G;
   constexpr int KB = KeyBits<K>::kBits;
   constexpr uint32_t KMASK = KeyBits<K>::kMask;
@@ -180,7 +200,8 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
   unsigned long long best = 0ull;
   int overflow = 0;
   const int nstrips = (M + RS - 1) / RS;
-  const int T_end = N + 2 * G - 1;
+  const int NP = S2 ? rmo.P : N;  // columns swept ([N, NP) score 0 in score2 mode)
+  const int T_end = NP + 2 * G - 1;
   const uint4 *tab = reinterpret_cast<const uint4 *>(gs.prof);
   const uint32_t zmask = lane == 0 ? 0u : 0xffffffffu;  // lane 0 sees the zero top boundary
   // 1 and 2^KB as values the compiler cannot fold (gs.pad is a launch argument >= 0)
@@ -196,10 +217,12 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
       for (int c = 0; c < L::kCodes; c++) {
 #pragma unroll
         for (int w = 0; w < K; w++) {
-          const uint32_t vlo = (uint32_t)(sub_score(A.code(row0 + w), c, sc, sc.gap_open) + sc.gap_open) & 0xffffu;
-          const uint32_t vhi = ((uint32_t)(sub_score(A.code(row0 + K + w), c, sc, sc.gap_open) + sc.gap_open) &
-                                0xffffu)
-                               << 16;
+          const int alo = A.code(row0 + w), ahi = A.code(row0 + K + w);
+          // the zero code scores 0 against real rows (biased gO); rows past A stay at -gO
+          const int slo = (S2 && c == kCode16Zero) ? (alo == kCodePad ? -sc.gap_open : 0) : sub_score(alo, c, sc, sc.gap_open);
+          const int shi = (S2 && c == kCode16Zero) ? (ahi == kCodePad ? -sc.gap_open : 0) : sub_score(ahi, c, sc, sc.gap_open);
+          const uint32_t vlo = (uint32_t)(slo + sc.gap_open) & 0xffffu;
+          const uint32_t vhi = ((uint32_t)(shi + sc.gap_open) & 0xffffu) << 16;
           tw[((c * L::kNV + L::lo_vec(w)) * G + lane) * 4 + L::lo_elem(w)] = vlo;
           tw[((c * L::kNV + L::hi_vec(w)) * G + lane) * 4 + L::hi_elem(w)] = vhi;
         }
@@ -219,20 +242,35 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
     uint32_t Zout = 0u;  // (lo: H of the hi-last row, hi: E^ below it)
     uint32_t Kl = 0u;    // running key per half
     uint32_t Jp = 0u;    // step of the last strict increase of Kl, per half
+    uint32_t Rm[K];      // score2 mode: running row maxima over valid columns
+#pragma unroll
+    for (int k = 0; k < K; k++) Rm[k] = 0u;
     const bool first_strip = (s == 0);
     const bool last_strip = (s == nstrips - 1);
     const int j0 = -2 * lane;  // lo column at step 0
-    int cnext = (j0 >= 0 && j0 < N) ? (int)bg[j0] : kCodeN;
+    auto code_at = [&](int j) -> int {
+      if ((unsigned)j < (unsigned)N) return (int)bg[j];
+      return (S2 && (unsigned)j < (unsigned)NP) ? kCode16Zero : kCodeN;
+    };
+    // score2 mode: 0 in a half whose column is inside [0, NP) at step t, else -16384
+    auto vmask_at = [&](int t) -> uint32_t {
+      if constexpr (!S2) return 0u;
+      const int jl = t + j0;
+      const uint32_t lo = (unsigned)jl < (unsigned)NP ? 0u : 0x0000C000u;
+      const uint32_t hi = (unsigned)(jl - 1) < (unsigned)NP ? 0u : 0xC0000000u;
+      return lo | hi;
+    };
+    int cnext = code_at(j0);
 
     auto top = [&](int t, uint32_t zs) -> uint32_t {
       uint32_t z = zs & zmask;
-      if (MULTI && lane == 0 && !first_strip && t < N) z = bnd[t];
+      if (MULTI && lane == 0 && !first_strip && t < NP) z = bnd[t];
       return z;
     };
     auto out_bnd = [&](int t) {
       if (MULTI && !last_strip && lane == G - 1) {
         const int jh = t - 2 * lane - 1;  // hi-half column of the last lane
-        if (jh >= 0 && jh < N) bnd[jh] = Zout;
+        if (jh >= 0 && jh < NP) bnd[jh] = Zout;
       }
     };
     int t = 0;
@@ -240,27 +278,36 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
       // even step: hi words into HA; the high half uses HB (previous column)
       int c = cnext;
       int jn = t + 1 + j0;
-      cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodeN;
+      cnext = code_at(jn);
       ST::load(tab, c, lane, Wlo, HA);
       uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
-      ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale);
+      ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale, Rm, vmask_at(t));
       out_bnd(t);
       // odd step: hi words into HB; the high half uses HA
       c = cnext;
       jn = t + 2 + j0;
-      cnext = ((unsigned)jn < (unsigned)N) ? (int)bg[jn] : kCodeN;
+      cnext = code_at(jn);
       ST::load(tab, c, lane, Wlo, HB);
       z = top(t + 1, __shfl_up_sync(gmask, Zout, 1, G));
-      ST::run(t + 1, z, Wlo, HA, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale);
+      ST::run(t + 1, z, Wlo, HA, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale, Rm,
+              vmask_at(t + 1));
       out_bnd(t + 1);
     }
     if (t < T_end) {
       ST::load(tab, cnext, lane, Wlo, HA);
       const uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
-      ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale);
+      ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale, Rm, vmask_at(t));
       out_bnd(t);
     }
 
+    if constexpr (S2) {
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        const int rl = row0 + k, rh = row0 + K + k;
+        if (rl < M) rmo.rowmax[rl] = (int32_t)(Rm[k] & 0xffffu);
+        if (rh < M) rmo.rowmax[rh] = (int32_t)(Rm[k] >> 16);
+      }
+    }
     // Decode the two halves' keys into (value, row, column) and reduce over the group.
     unsigned long long kbest = 0ull;
     int vmax_lane = 0;
@@ -292,13 +339,14 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
   out.overflow = overflow;
 }
 
-template <int K, int G>
+template <int K, int G, bool S2 = false>
 __device__ __forceinline__ void sweep16(const SeqView &A, const SeqView &B, const Scoring &sc, const GroupSmem &gs,
-                                        int lane, unsigned gmask, V16::Pay *bnd, int ceiling, SweepOut &out) {
+                                        int lane, unsigned gmask, V16::Pay *bnd, int ceiling, SweepOut &out,
+                                        const RowMaxOut &rmo = RowMaxOut{nullptr, 0}) {
   if (A.len > 2 * K * G)
-    sweep16_impl<K, G, true>(A, B, sc, gs, lane, gmask, bnd, ceiling, out);
+    sweep16_impl<K, G, true, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, out, rmo);
   else
-    sweep16_impl<K, G, false>(A, B, sc, gs, lane, gmask, bnd, ceiling, out);
+    sweep16_impl<K, G, false, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, out, rmo);
 }
 
 }  // namespace mhsw

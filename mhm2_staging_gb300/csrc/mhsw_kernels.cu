@@ -36,7 +36,7 @@ __device__ __forceinline__ unsigned group_mask(int G) {
   return ((1u << G) - 1u) << ((lane32 / G) * G);
 }
 
-template <class VT, int K, int G>
+template <class VT, int K, int G, bool S2 = false>
 __global__ void __launch_bounds__(256) k_fwd(PairSet ps, ResultSet rs, Scoring sc, const int64_t *__restrict__ list,
                                              const int *__restrict__ list_count, int ceiling,
                                              typename VT::Pay *scratch, int scratch_stride, WorkLists wl, int pad,
@@ -70,7 +70,8 @@ __global__ void __launch_bounds__(256) k_fwd(PairSet ps, ResultSet rs, Scoring s
   for (int64_t i = gid; i < total; i += gstride) {
     const int64_t p = list ? list[i] : i;
     const int M = ps.a_len[p], N = ps.b_len[p];
-    const bool too_long = (N > bcap - pad - 2 * G) || (M > RS && (bnd == nullptr || N > scratch_stride));
+    const int NP = S2 ? ssw_pad16(N) : N;  // columns swept (score2 mode adds SSW's padding)
+    const bool too_long = (NP > bcap - pad - 2 * G) || (M > RS && (bnd == nullptr || NP > scratch_stride));
     if (M <= 0 || N <= 0 || too_long) {
       if (lane == 0) {
         rs.score[p] = 0;
@@ -83,7 +84,9 @@ __global__ void __launch_bounds__(256) k_fwd(PairSet ps, ResultSet rs, Scoring s
     SeqView A{ps.a_code + ps.a_off[p], 1, M};
     SeqView B{ps.b_code + ps.b_off[p], 1, N};
     SweepOut so;
-    sweep_pair<VT, K, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so);
+    RowMaxOut2 rm2{nullptr, nullptr, 0, 0};
+    if constexpr (S2) rm2 = RowMaxOut2{ps.rowmax16 + ps.a_off[p], ps.rowmax8 + ps.a_off[p], NP, ssw_pad8(N)};
+    sweep_pair<VT, K, G, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, so, rm2);
     if (lane == 0) {
       const int S = key_value(so.key);
       if (!kWide && so.overflow) {
@@ -105,7 +108,7 @@ __global__ void __launch_bounds__(256) k_fwd(PairSet ps, ResultSet rs, Scoring s
 
 // Plain forward pass with the keyed int16 engine (mhsw_engine16.cuh): one G-lane group
 // per pair, grid-stride over [0, n).
-template <int K, int G>
+template <int K, int G, bool S2 = false>
 __global__ void __launch_bounds__(256) k_fwd16(PairSet ps, ResultSet rs, Scoring sc, int ceiling, V16::Pay *scratch,
                                                int scratch_stride, WorkLists wl, int pad, int bcap) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -113,7 +116,7 @@ __global__ void __launch_bounds__(256) k_fwd16(PairSet ps, ResultSet rs, Scoring
   const int grp = threadIdx.x / G;
   const int lane = threadIdx.x % G;
   const unsigned gmask = group_mask(G);
-  constexpr size_t kProf = group_prof16_bytes<K, G>();
+  constexpr size_t kProf = group_prof16_bytes<K, G, S2 ? kCode16Zero + 1 : kCodeN + 1>();
   unsigned char *gbase = smem + (size_t)grp * kProf;  // keyed engine: profile table only
   GroupSmem gs;
   gs.prof = reinterpret_cast<uint32_t *>(gbase);
@@ -127,7 +130,8 @@ __global__ void __launch_bounds__(256) k_fwd16(PairSet ps, ResultSet rs, Scoring
   V16::Pay *bnd = scratch ? scratch + gid * (int64_t)scratch_stride : nullptr;
   for (int64_t p = gid; p < ps.n; p += gstride) {
     const int M = ps.a_len[p], N = ps.b_len[p];
-    const bool too_long = (N > kMaxB) || (M > RS && (bnd == nullptr || N > scratch_stride));
+    const int NP = S2 ? ssw_pad16(N) : N;
+    const bool too_long = (N > kMaxB) || (M > RS && (bnd == nullptr || NP > scratch_stride));
     if (M <= 0 || N <= 0 || too_long) {
       if (lane == 0) {
         rs.score[p] = 0;
@@ -140,10 +144,15 @@ __global__ void __launch_bounds__(256) k_fwd16(PairSet ps, ResultSet rs, Scoring
     SeqView A{ps.a_code + ps.a_off[p], 1, M};
     SeqView B{ps.b_code + ps.b_off[p], 1, N};
     SweepOut so;
-    sweep16<K, G>(A, B, sc, gs, lane, gmask, bnd, ceiling, so);
+    RowMaxOut rmo{nullptr, 0};
+    if constexpr (S2) rmo = RowMaxOut{ps.rowmax16 + ps.a_off[p], NP};
+    sweep16<K, G, S2>(A, B, sc, gs, lane, gmask, bnd, ceiling, so, rmo);
     if (lane == 0) {
       const int S = key_value(so.key);
-      if (so.overflow) {
+      // score2 mode: SSW's word path pads B to a multiple of 8; where that differs from
+      // the byte-path padding swept here, the int32 pass recomputes the row maxima.
+      const bool word_redo = S2 && S + ssw_bias(sc) >= 255 && ssw_pad8(N) != NP;
+      if (so.overflow || word_redo) {
         rs.flag[p] = kFlagOverflow16;
         const int slot = atomicAdd(wl.ovf_count, 1);
         if (slot < wl.cap) wl.ovf[slot] = p;
@@ -397,6 +406,42 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
   }
 }
 
+// SSW's second-best score (ssw_core.cpp:513-536, :825-847, :1154-1160) from the row
+// maxima of the forward pass: the largest row maximum, first row on ties, over rows
+// before a_end - maskLen and from a_end + maskLen on (+1 on the byte path), with
+// maskLen = max(len(A)/2, 15) as klign passes it (klign.cpp:257).
+__global__ void k_score2(PairSet ps, ResultSet rs, Scoring sc, int64_t n) {
+  const int bias = ssw_bias(sc);
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int M = ps.a_len[p], N = ps.b_len[p];
+    int best = 0, at = 0;
+    if (M > 0 && N > 0 && !(rs.flag[p] & kFlagTooLong)) {
+      const int S = rs.score[p], ie = rs.a_end[p];
+      const int mask = M / 2 > 15 ? M / 2 : 15;
+      const bool word = S + bias >= 255;
+      const int32_t *rm = ((word && ssw_pad8(N) != ssw_pad16(N)) ? ps.rowmax8 : ps.rowmax16) + ps.a_off[p];
+      const int e1 = ie - mask > 0 ? ie - mask : 0;
+      for (int i = 0; i < e1; i++) {
+        const int v = rm[i];
+        if (v > best) {
+          best = v;
+          at = i;
+        }
+      }
+      const int e2 = ie + mask > M ? M : ie + mask;
+      for (int i = word ? e2 : e2 + 1; i < M; i++) {
+        const int v = rm[i];
+        if (v > best) {
+          best = v;
+          at = i;
+        }
+      }
+    }
+    rs.score2[p] = best;
+    rs.a_end2[p] = at;
+  }
+}
+
 // Byte arena -> SSW base codes (0..4), 16 bytes per thread step when aligned.
 __global__ void k_translate(const char *__restrict__ src, uint8_t *__restrict__ dst, int64_t nbytes, int vec) {
   __shared__ uint8_t tab[256];
@@ -541,16 +586,21 @@ int num_sms(int device) {
   return g_num_sms;
 }
 
-size_t group_prof16_rt(int K, int G) {
+template <int C>
+size_t group_prof16_rt_c(int K, int G) {
   if (G == kGKShort) {
     switch (K) {
-      case 4: return group_prof16_bytes<4, kGKShort>();
-      case 6: return group_prof16_bytes<6, kGKShort>();
-      case 8: return group_prof16_bytes<8, kGKShort>();
-      default: return group_prof16_bytes<10, kGKShort>();
+      case 4: return group_prof16_bytes<4, kGKShort, C>();
+      case 6: return group_prof16_bytes<6, kGKShort, C>();
+      case 8: return group_prof16_bytes<8, kGKShort, C>();
+      default: return group_prof16_bytes<10, kGKShort, C>();
     }
   }
-  return K == 6 ? group_prof16_bytes<6, kGKLong>() : group_prof16_bytes<8, kGKLong>();
+  return K == 6 ? group_prof16_bytes<6, kGKLong, C>() : group_prof16_bytes<8, kGKLong, C>();
+}
+
+size_t group_prof16_rt(int K, int G, bool s2) {
+  return s2 ? group_prof16_rt_c<kCode16Zero + 1>(K, G) : group_prof16_rt_c<kCodeN + 1>(K, G);
 }
 
 size_t group_prof_rt(bool wide32, int K) {
@@ -570,7 +620,7 @@ template <class VT, int K>
 cudaError_t launch_fwd_t(const FwdConfig &cfg, const PairSet &ps, const ResultSet &rs, const Scoring &sc,
                          const int64_t *list, const int *list_count, int ceiling, void *scratch, int scratch_stride,
                          const WorkLists &wl, cudaStream_t st) {
-  auto kern = k_fwd<VT, K, kG>;
+  auto kern = ps.rowmax16 ? k_fwd<VT, K, kG, true> : k_fwd<VT, K, kG, false>;
   {
     cudaError_t e = raise_smem_limit(reinterpret_cast<const void *>(kern), cfg.smem);
     if (e != cudaSuccess) return e;
@@ -584,7 +634,7 @@ cudaError_t launch_fwd_t(const FwdConfig &cfg, const PairSet &ps, const ResultSe
 template <int K, int G>
 cudaError_t launch_fwd16_t(const FwdConfig &cfg, const PairSet &ps, const ResultSet &rs, const Scoring &sc,
                            int ceiling, void *scratch, int scratch_stride, const WorkLists &wl, cudaStream_t st) {
-  auto kern = k_fwd16<K, G>;
+  auto kern = ps.rowmax16 ? k_fwd16<K, G, true> : k_fwd16<K, G, false>;
   {
     cudaError_t e = raise_smem_limit(reinterpret_cast<const void *>(kern), cfg.smem);
     if (e != cudaSuccess) return e;
@@ -601,7 +651,7 @@ bool keyed_scoring(const Scoring &sc) {
   return sc.mismatch <= sc.gap_open && sc.ambiguity <= sc.gap_open && sc.gap_open >= 1 && sc.gap_extend >= 1;
 }
 
-cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg, bool keyed) {
+cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg, bool keyed, bool s2) {
   FwdConfig c{};
   c.G = kG;
   if (keyed && !wide32) {
@@ -622,11 +672,12 @@ cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfi
   c.pad = 2 * c.G;
   if (max_b < 1) max_b = 1;
   if (max_b > kMaxB) return cudaErrorInvalidValue;
-  c.bcap = ((c.pad + max_b + 2 * c.G) + 15) / 16 * 16;
+  // room for B, the groups' lane skew and SSW's zero-score padding of score2 mode (< 16)
+  c.bcap = ((c.pad + max_b + 16 + 2 * c.G) + 15) / 16 * 16;
   const size_t budget = 100 * 1024;  // keep two blocks per SM possible
   // the keyed engine reads B from global memory: its group needs the profile table only
   const size_t per_group =
-      (keyed && !wide32) ? group_prof16_rt(c.K, c.G) : group_prof_rt(wide32, c.K) + (size_t)c.bcap;
+      (keyed && !wide32) ? group_prof16_rt(c.K, c.G, s2) : group_prof_rt(wide32, c.K) + (size_t)c.bcap;
   int gpb = 8;
   while (gpb > 1 && (size_t)gpb * per_group > budget) gpb /= 2;
   if (c.G < kG) gpb *= kG / c.G;  // same block size (128 threads) with smaller groups
@@ -790,6 +841,13 @@ cudaError_t launch_translate(const char *src, uint8_t *dst, int64_t nbytes, cuda
   const int64_t work = vec ? (nbytes / 16 + 1) : nbytes;
   const int grid = (int)std::min<int64_t>((work + 255) / 256, 152 * 16);
   k_translate<<<grid, 256, 0, st>>>(src, dst, nbytes, vec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_score2(const PairSet &ps, const ResultSet &rs, const Scoring &sc, cudaStream_t st) {
+  if (ps.n <= 0) return cudaSuccess;
+  const int grid = (int)std::min<int64_t>((ps.n + 255) / 256, 4096);
+  k_score2<<<grid, 256, 0, st>>>(ps, rs, sc, ps.n);
   return cudaGetLastError();
 }
 

@@ -61,7 +61,11 @@ cudaError_t raise_smem_limit(const void *func, size_t bytes);
 
 // Chooses K/G/grid/smem for a forward launch over pairs whose A (rows) lengths are at
 // most max_a and B lengths at most max_b.  wide32 selects the int32 engine.
-cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg, bool keyed = false);
+// s2: score2 mode (the keyed profile table gains the zero-score code).
+cudaError_t plan_forward(int device, int max_a, int max_b, bool wide32, FwdConfig *cfg, bool keyed = false,
+                         bool s2 = false);
+// Second-best scores (score2 mode) from the row maxima the forward pass wrote.
+cudaError_t launch_score2(const PairSet &ps, const ResultSet &rs, const Scoring &sc, cudaStream_t st);
 
 // Bytes of strip scratch a forward launch needs (0 when A fits one strip).
 size_t forward_scratch_bytes(const FwdConfig &cfg, int max_a, int max_b, bool wide32);

@@ -41,6 +41,8 @@ class _AlnResults(C.Structure):
         ("query_end32", C.POINTER(C.c_int32)),
         ("top_scores32", C.POINTER(C.c_int32)),
         ("n", C.c_int32),
+        ("score2_32", C.POINTER(C.c_int32)),
+        ("a_end2_32", C.POINTER(C.c_int32)),
     ]
 
 
@@ -149,6 +151,8 @@ SIGNATURES: dict[str, tuple] = {
     "mhsw_driver_set_form": (C.c_int, [_P, C.c_int]),
     "mhsw_driver_set_int16_ceiling": (C.c_int, [_P, C.c_int]),
     "mhsw_driver_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "mhsw_driver_set_score2": (C.c_int, [_P, C.c_int]),
+    "mhsw_last_score2": (C.c_int, [_P, _P, _P, C.c_int]),
     "mhsw_run_kernel_forwards": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32, C.c_uint32, C.c_uint32]),
     "mhsw_run_kernel_backwards": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32, C.c_uint32, C.c_uint32]),
     "mhsw_kernel_is_done": (C.c_int, [_P, C.POINTER(C.c_int)]),
@@ -286,6 +290,8 @@ class AlignmentResults:
     ref_end32: np.ndarray
     query_end32: np.ndarray
     top_scores32: np.ndarray
+    score2: np.ndarray | None = None  # score2 mode: SSW's second-best score
+    a_end2: np.ndarray | None = None  # and its A row (the read row in klign's orientation)
 
 
 def _as_bytes_list(seqs: Sequence[str | bytes]) -> list[bytes]:
@@ -330,6 +336,18 @@ class GPUDriver:
 
     def set_int16_ceiling(self, ceiling: int) -> None:
         self._ck(self._lib.mhsw_driver_set_int16_ceiling(self._h, ceiling), "set_int16_ceiling")
+
+    def set_score2(self, on: bool) -> None:
+        """Score2 mode: also compute SSW's second-best score (klign's aln.score2)."""
+        self._ck(self._lib.mhsw_driver_set_score2(self._h, 1 if on else 0), "set_score2")
+
+    def last_score2(self, n: int) -> np.ndarray:
+        """n x 2 int32 (score2, its A row) of the last batch aligned in score2 mode."""
+        s2 = np.zeros(n, dtype=np.int32)
+        a2 = np.zeros(n, dtype=np.int32)
+        self._ck(self._lib.mhsw_last_score2(self._h, s2.ctypes.data if n else None, a2.ctypes.data if n else None, 1),
+                 "last_score2")
+        return np.stack([s2, a2], axis=1)
 
     def stream(self) -> int:
         s = _P()
@@ -389,7 +407,8 @@ class GPUDriver:
             arr(r.ref_begin, np.int16), arr(r.query_begin, np.int16), arr(r.ref_end, np.int16),
             arr(r.query_end, np.int16), arr(r.top_scores, np.int16), arr(r.ref_begin32, np.int32),
             arr(r.query_begin32, np.int32), arr(r.ref_end32, np.int32), arr(r.query_end32, np.int32),
-            arr(r.top_scores32, np.int32))
+            arr(r.top_scores32, np.int32),
+            arr(r.score2_32, np.int32) if r.score2_32 else None, arr(r.a_end2_32, np.int32) if r.a_end2_32 else None)
 
     # ---- batch entry point ---------------------------------------------------------
     def align_pairs(self, pairs: "Pairs", form: int = FORM_PLAIN, out: np.ndarray | None = None,
