@@ -222,7 +222,8 @@ def run_paths(drv, dev, torch, stream) -> dict:
     device (each: 2 warm-up calls, then 3 timed with CUDA events on the driver's stream):
     the 150/300 bp batch (plain and batched form), the 1M-pair read/ref mix with 30%
     unrelated reads, the 200k long-reference batch, and the 200k-pair slice of the uneven
-    batch with every pair re-run by the int32 engine (int16 ceiling 0)."""
+    batch with every pair re-run by the int32 engine (int16 ceiling 0), and the same slice in
+    score2 mode (SSW's second-best score as well)."""
     from mhm2_staging_gb300 import FORM_BATCHED, FORM_PLAIN, workloads
     from mhm2_staging_gb300.driver import DevicePairs, limits
 
@@ -231,7 +232,8 @@ def run_paths(drv, dev, torch, stream) -> dict:
              ("150bp_vs_300bp_10k_pairs_batched", 0, 10_000, FORM_BATCHED, None),
              ("reads_100_250bp_1M_pairs_30pct_unrelated", 1, 1_000_000, FORM_BATCHED, None),
              ("250bp_vs_2_8kb_refs_200k_pairs", 4, 200_000, FORM_BATCHED, None),
-             ("uneven_200k_pairs_all_int32", 2, 200_000, FORM_BATCHED, 0)]
+             ("uneven_200k_pairs_all_int32", 2, 200_000, FORM_BATCHED, 0),
+             ("uneven_200k_pairs_score2_mode", 2, 200_000, FORM_BATCHED, "score2")]
     default_ceiling = limits().int16_ceiling
     for name, cfg, n, form, ceiling in specs:
         pp = workloads.generate(cfg, n=n)
@@ -241,7 +243,9 @@ def run_paths(drv, dev, torch, stream) -> dict:
         dp = DevicePairs(*(t.data_ptr() for t in tens), n=pp.n, max_a_len=int(pp.a_len.max()),
                          max_b_len=int(pp.b_len.max()), cells=cells, a_bytes=int((pp.a_off + pp.a_len).max()),
                          b_bytes=int((pp.b_off + pp.b_len).max()))
-        drv.set_int16_ceiling(default_ceiling if ceiling is None else ceiling)
+        score2 = ceiling == "score2"
+        drv.set_score2(score2)
+        drv.set_int16_ceiling(default_ceiling if ceiling is None or score2 else ceiling)
         for _ in range(2):
             drv.align_pairs_device(dp, o.data_ptr(), form=form)
         torch.cuda.synchronize(dev)
@@ -262,6 +266,7 @@ def run_paths(drv, dev, torch, stream) -> dict:
         del tens, o
         torch.cuda.empty_cache()
     drv.set_int16_ceiling(default_ceiling)
+    drv.set_score2(False)
     return out
 
 
