@@ -45,6 +45,13 @@ def _bind(lib: C.CDLL, name: str) -> None:
                    C.c_int, _P]
 
 
+def _bind_cigar(lib: C.CDLL, name: str) -> None:
+    fn = getattr(lib, name)
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_char_p, _P, _P, C.c_char_p, _P, _P, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                   C.c_int, _P, _P, _P, C.c_int]
+
+
 def oracle_lib() -> C.CDLL:
     global _ORACLE
     if _ORACLE is None:
@@ -53,6 +60,7 @@ def oracle_lib() -> C.CDLL:
         lib = C.CDLL(str(ORACLE_SO))
         _bind(lib, "sw_oracle_align_batch")
         _bind(lib, "sw_oracle_align_batch7")
+        _bind_cigar(lib, "sw_oracle_cigar_batch")
         lib.sw_oracle_align_codes.restype = C.c_int64
         lib.sw_oracle_align_codes.argtypes = [_P, C.c_int, _P, C.c_int, _P, C.c_int, C.c_int, _P]
         _ORACLE = lib
@@ -71,6 +79,7 @@ def ref_lib() -> C.CDLL:
         lib = C.CDLL(str(REF_SO))
         _bind(lib, "ssw_ref_align_batch")
         _bind(lib, "ssw_ref_align_batch7")
+        _bind_cigar(lib, "ssw_ref_cigar_batch")
         lib.ssw_ref_align.restype = C.c_int
         lib.ssw_ref_align.argtypes = [C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_int, C.c_int, _P]
@@ -107,6 +116,42 @@ def ref_align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, 
     if score2:
         return _run(ref_lib(), "ssw_ref_align_batch7", pairs, scoring, threads or (os.cpu_count() or 1), 7)
     return _run(ref_lib(), "ssw_ref_align_batch", pairs, scoring, threads or (os.cpu_count() or 1))
+
+
+def _run_cigar(lib, fn, pairs, scoring, threads, ops_cap):
+    n = pairs.n
+    out = np.zeros((n, 6), dtype=np.int32)
+    ops = np.zeros((n, ops_cap), dtype=np.uint32)
+    nops = np.zeros(n, dtype=np.int32)
+    if n == 0:
+        return out, ops, nops
+    m, x, go, ge, amb = scoring
+    rc = getattr(lib, fn)(pairs.a_seq.ctypes.data_as(C.c_char_p), pairs.a_off.ctypes.data, pairs.a_len.ctypes.data,
+                          pairs.b_seq.ctypes.data_as(C.c_char_p), pairs.b_off.ctypes.data, pairs.b_len.ctypes.data,
+                          n, m, x, go, ge, amb, threads, out.ctypes.data, ops.ctypes.data, nops.ctypes.data, ops_cap)
+    if rc != 0:
+        raise RuntimeError(f"{fn} failed")
+    return out, ops, nops
+
+
+def cigar_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, ops_cap: int = 256):
+    """Oracle alignments with CIGARs (SSW's Filter(true, true, 0, 32767)): returns
+    (out n x 6 = score, a_begin, a_end, b_begin, b_end, mismatches; ops n x ops_cap
+    BAM-encoded ops; nops n = op count, 0 for none, -1 when over ops_cap)."""
+    return _run_cigar(oracle_lib(), "sw_oracle_cigar_batch", pairs, scoring, threads or (os.cpu_count() or 1), ops_cap)
+
+
+def ref_cigar_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, ops_cap: int = 256):
+    """The reference SSW with report_cigar, same layout as cigar_batch."""
+    return _run_cigar(ref_lib(), "ssw_ref_cigar_batch", pairs, scoring, threads or (os.cpu_count() or 1), ops_cap)
+
+
+CIGAR_OPS = "MIDNSHP=X"
+
+
+def cigar_string(ops_row, n: int) -> str:
+    """SAM text of n BAM-encoded ops."""
+    return "".join(f"{int(c) >> 4}{CIGAR_OPS[int(c) & 15]}" for c in ops_row[:n])
 
 
 def ref_align_one(query: bytes, ref: bytes, scoring=(1, 3, 5, 2, 2), mask_len: int = -1) -> list[int]:

@@ -138,4 +138,90 @@ int ssw_ref_align_batch7(const char *a_seqs, const int64_t *a_off, const int32_t
                        nthreads, out, 7);
 }
 
+// With report_cigar (Filter(true, true, 0, 32767), the filter klign's post-assembly
+// alignment asks for): out[6p..6p+5] = score, a_begin, a_end, b_begin, b_end, mismatches;
+// ops[ops_cap*p ..] = the BAM-encoded CIGAR, nops[p] its length (-1: more than ops_cap).
+struct RefCigarBatch {
+  const char *a_seqs, *b_seqs;
+  const int64_t *a_off, *b_off;
+  const int32_t *a_len, *b_len;
+  int64_t n;
+  int match, mismatch, gO, gE, amb;
+  int32_t *out;
+  uint32_t *ops;
+  int32_t *nops;
+  int ops_cap;
+  int64_t next;
+  pthread_mutex_t mu;
+};
+
+static void *ref_cigar_worker(void *arg) {
+  RefCigarBatch *bt = (RefCigarBatch *)arg;
+  Aligner aligner((uint8_t)bt->match, (uint8_t)bt->mismatch, (uint8_t)bt->gO, (uint8_t)bt->gE, (uint8_t)bt->amb);
+  Filter filter(true, true, 0, 32767);
+  Alignment aln;
+  std::string q;
+  for (;;) {
+    pthread_mutex_lock(&bt->mu);
+    int64_t lo = bt->next;
+    bt->next += 64;
+    pthread_mutex_unlock(&bt->mu);
+    if (lo >= bt->n) break;
+    int64_t hi = lo + 64 < bt->n ? lo + 64 : bt->n;
+    for (int64_t p = lo; p < hi; p++) {
+      q.assign(bt->b_seqs + bt->b_off[p], (size_t)bt->b_len[p]);
+      int rl = bt->a_len[p];
+      int mask_len = rl / 2 > 15 ? rl / 2 : 15;
+      aln.Clear();
+      aligner.Align(q.c_str(), bt->a_seqs + bt->a_off[p], rl, filter, &aln, mask_len);
+      int32_t *o = bt->out + 6 * p;
+      o[0] = aln.sw_score;
+      o[1] = aln.ref_begin;
+      o[2] = aln.ref_end;
+      o[3] = aln.query_begin;
+      o[4] = aln.query_end;
+      o[5] = aln.mismatches;
+      if ((int64_t)aln.cigar.size() > bt->ops_cap) {
+        bt->nops[p] = -1;
+      } else {
+        bt->nops[p] = (int32_t)aln.cigar.size();
+        for (size_t k = 0; k < aln.cigar.size(); k++) bt->ops[(int64_t)bt->ops_cap * p + (int64_t)k] = aln.cigar[k];
+      }
+    }
+  }
+  return nullptr;
+}
+
+int ssw_ref_cigar_batch(const char *a_seqs, const int64_t *a_off, const int32_t *a_len, const char *b_seqs,
+                        const int64_t *b_off, const int32_t *b_len, int64_t n, int match, int mismatch, int gap_open,
+                        int gap_extend, int ambiguity, int nthreads, int32_t *out, uint32_t *ops, int32_t *nops,
+                        int ops_cap) {
+  RefCigarBatch bt;
+  bt.a_seqs = a_seqs;
+  bt.b_seqs = b_seqs;
+  bt.a_off = a_off;
+  bt.b_off = b_off;
+  bt.a_len = a_len;
+  bt.b_len = b_len;
+  bt.n = n;
+  bt.match = match;
+  bt.mismatch = mismatch;
+  bt.gO = gap_open;
+  bt.gE = gap_extend;
+  bt.amb = ambiguity;
+  bt.out = out;
+  bt.ops = ops;
+  bt.nops = nops;
+  bt.ops_cap = ops_cap;
+  bt.next = 0;
+  pthread_mutex_init(&bt.mu, nullptr);
+  if (nthreads < 1) nthreads = 1;
+  std::vector<pthread_t> th((size_t)nthreads);
+  for (int t = 1; t < nthreads; t++) pthread_create(&th[t], nullptr, ref_cigar_worker, &bt);
+  ref_cigar_worker(&bt);
+  for (int t = 1; t < nthreads; t++) pthread_join(th[t], nullptr);
+  pthread_mutex_destroy(&bt.mu);
+  return 0;
+}
+
 }  // extern "C"

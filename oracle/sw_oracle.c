@@ -225,9 +225,15 @@ typedef struct {
   int32_t *out;
   int64_t next;
   int64_t chunk;
-  int width; /* 5: score and coordinates; 7: plus score2 and a_end2 */
+  int width; /* 5: score and coordinates; 7: plus score2 and a_end2; 6: plus mismatches, with CIGARs */
+  uint32_t *ops;  /* width 6: ops_cap BAM-encoded CIGAR ops per pair */
+  int32_t *nops;  /* width 6: op count per pair, -1 when more than ops_cap */
+  int ops_cap;
   pthread_mutex_t mu;
 } swo_batch;
+
+int sw_oracle_cigar(const uint8_t *A, int M, const uint8_t *B, int N, const int8_t *mat, int gO, int gE,
+                    const int32_t *res5, uint32_t *ops, int cap, int32_t *mismatches);
 
 static void *swo_worker(void *arg) {
   swo_batch *bt = (swo_batch *)arg;
@@ -254,7 +260,12 @@ static void *swo_worker(void *arg) {
       }
       sw_oracle_encode(bt->a_seqs + bt->a_off[p], la, ca);
       sw_oracle_encode(bt->b_seqs + bt->b_off[p], lb, cb);
-      if (bt->width == 7) {
+      if (bt->width == 6) {
+        int32_t *o = bt->out + 6 * p;
+        sw_oracle_align_codes(ca, la, cb, lb, bt->mat, bt->gO, bt->gE, o);
+        bt->nops[p] = sw_oracle_cigar(ca, la, cb, lb, bt->mat, bt->gO, bt->gE, o, bt->ops + (int64_t)bt->ops_cap * p,
+                                      bt->ops_cap, o + 5);
+      } else if (bt->width == 7) {
         const int mask_len = la / 2 > 15 ? la / 2 : 15;
         sw_oracle_align_codes7(ca, la, cb, lb, bt->mat, bt->gO, bt->gE, mask_len, bt->out + 7 * p);
       } else {
@@ -271,7 +282,8 @@ static void *swo_worker(void *arg) {
  * B_p likewise.  out is n*5 int32 (score, a_begin, a_end, b_begin, b_end). */
 static int swo_batch_run(const char *a_seqs, const int64_t *a_off, const int32_t *a_len, const char *b_seqs,
                          const int64_t *b_off, const int32_t *b_len, int64_t n, int match, int mismatch, int gap_open,
-                         int gap_extend, int ambiguity, int nthreads, int32_t *out, int width) {
+                         int gap_extend, int ambiguity, int nthreads, int32_t *out, int width, uint32_t *ops,
+                         int32_t *nops, int ops_cap) {
   swo_batch bt;
   bt.width = width;
   bt.a_seqs = a_seqs;
@@ -285,6 +297,9 @@ static int swo_batch_run(const char *a_seqs, const int64_t *a_off, const int32_t
   bt.gO = gap_open;
   bt.gE = gap_extend;
   bt.out = out;
+  bt.ops = ops;
+  bt.nops = nops;
+  bt.ops_cap = ops_cap;
   bt.next = 0;
   bt.chunk = 64;
   pthread_mutex_init(&bt.mu, NULL);
@@ -302,7 +317,7 @@ int sw_oracle_align_batch(const char *a_seqs, const int64_t *a_off, const int32_
                           const int64_t *b_off, const int32_t *b_len, int64_t n, int match, int mismatch, int gap_open,
                           int gap_extend, int ambiguity, int nthreads, int32_t *out) {
   return swo_batch_run(a_seqs, a_off, a_len, b_seqs, b_off, b_len, n, match, mismatch, gap_open, gap_extend, ambiguity,
-                       nthreads, out, 5);
+                       nthreads, out, 5, NULL, NULL, 0);
 }
 
 /* As sw_oracle_align_batch with out = n*7 int32: score, a_begin, a_end, b_begin, b_end,
@@ -311,5 +326,202 @@ int sw_oracle_align_batch7(const char *a_seqs, const int64_t *a_off, const int32
                            const int64_t *b_off, const int32_t *b_len, int64_t n, int match, int mismatch, int gap_open,
                            int gap_extend, int ambiguity, int nthreads, int32_t *out) {
   return swo_batch_run(a_seqs, a_off, a_len, b_seqs, b_off, b_len, n, match, mismatch, gap_open, gap_extend, ambiguity,
-                       nthreads, out, 7);
+                       nthreads, out, 7, NULL, NULL, 0);
+}
+
+/* ---- CIGAR (report_cigar = true) ----------------------------------------------------
+ * Restates what SSW returns when the filter asks for a CIGAR:
+ *  1. banded_sw (ssw_core.cpp:854-1053) on the aligned boxes A[a_begin..a_end] (its "ref",
+ *     columns j) and B[b_begin..b_end] (its "read", rows i): a banded DP whose band
+ *     half-width starts at |lenA - lenB| + 1 and doubles until the box's maximum reaches
+ *     the score, with the band kept left-aligned per row (index j - max(i - w, 0) + 1,
+ *     ssw_core.cpp:99-102) and its edge cell cleared at each row start exactly as SSW
+ *     does; three direction codes per cell; a traceback from the box's last cell that
+ *     stops at row 0 and closes with an M of one more (or a separate 1M);
+ *  2. ConvertAlignment (ssw.cpp:57-93): soft clips for the unaligned ends of B;
+ *  3. CalculateNumberMismatch (ssw.cpp:129-254): every M split into = / X by comparing
+ *     base codes (N against N counts as equal there), mismatches = X + I + D lengths.
+ * Ops are BAM-encoded, length << 4 | op with M=0 I=1 D=2 S=4 '='=7 X=8. */
+enum { SWO_OP_M = 0, SWO_OP_I = 1, SWO_OP_D = 2, SWO_OP_S = 4, SWO_OP_EQ = 7, SWO_OP_X = 8 };
+
+static int swo_push(uint32_t *ops, int cap, int *n, uint32_t len, int op) {
+  if (*n >= cap) return -1;
+  ops[(*n)++] = (len << 4) | (uint32_t)op;
+  return 0;
+}
+
+/* banded_sw's raw CIGAR (M/I/D, in order) for the boxes; returns the op count or -1. */
+static int swo_banded(const uint8_t *ref, int refLen, const uint8_t *read, int readLen, int score, const int8_t *mat,
+                      int gO, int gE, uint32_t *raw, int cap) {
+  int w = refLen > readLen ? refLen - readLen : readLen - refLen;
+  w += 1;
+  int max = 0;
+  int32_t *hb = NULL, *eb = NULL, *hc = NULL;
+  int8_t *dir = NULL;
+  int last_w = w;
+  for (;;) {
+    const int width = 2 * w + 3, width_d = 2 * w + 1;
+    free(hb);
+    free(eb);
+    free(hc);
+    free(dir);
+    hb = (int32_t *)calloc((size_t)width + 1, sizeof(int32_t));
+    eb = (int32_t *)calloc((size_t)width + 1, sizeof(int32_t));
+    hc = (int32_t *)calloc((size_t)width + 1, sizeof(int32_t));
+    dir = (int8_t *)calloc((size_t)width_d * 3 * (size_t)readLen + 16, 1);
+    for (int i = 0; i < readLen; i++) {
+      const int x0 = i - w > 0 ? i - w : 0;               /* band start (left-aligned storage) */
+      const int jb = x0, je = refLen - 1 < i + w ? refLen - 1 : i + w;
+      const int edge = je + 1 < width - 1 ? je + 1 : width - 1;
+      int f = 0;
+      hb[0] = eb[0] = hb[edge] = eb[edge] = hc[0] = 0;
+      int8_t *line = dir + (size_t)width_d * 3 * i;
+      const int xp = i - 1 - w > 0 ? i - 1 - w : 0;      /* previous row's band start */
+      int u = 0;
+      for (int j = jb; j <= je; j++) {
+        u = j - x0 + 1;
+        const int e = j - xp + 1, b = u - 1, d = e - 1;
+        const int dbase = (j - x0) * 3;
+        int t1 = i == 0 ? -gO : hb[e] - gO;
+        int t2 = i == 0 ? -gE : eb[e] - gE;
+        eb[u] = t1 > t2 ? t1 : t2;
+        line[dbase + 0] = (int8_t)(t1 > t2 ? 3 : 2);
+        t1 = hc[b] - gO;
+        t2 = f - gE;
+        f = t1 > t2 ? t1 : t2;
+        line[dbase + 1] = (int8_t)(t1 > t2 ? 5 : 4);
+        const int e1 = eb[u] > 0 ? eb[u] : 0, f1 = f > 0 ? f : 0;
+        t1 = e1 > f1 ? e1 : f1;
+        t2 = hb[d] + mat[ref[j] * 5 + read[i]];
+        hc[u] = t1 > t2 ? t1 : t2;
+        if (hc[u] > max) max = hc[u];
+        line[dbase + 2] = (int8_t)(t1 <= t2 ? 1 : (e1 > f1 ? line[dbase + 0] : line[dbase + 1]));
+      }
+      for (int k = 1; k <= u; k++) hb[k] = hc[k];
+    }
+    last_w = w;
+    w *= 2;
+    if (max >= score) break;
+    if (last_w > refLen + readLen + 2) { /* the full box never reaches the score: inconsistent input */
+      free(hb);
+      free(eb);
+      free(hc);
+      free(dir);
+      return -1;
+    }
+  }
+  const int bw = last_w, width_d = 2 * bw + 1;
+  /* traceback, ops collected last-to-first */
+  uint32_t *rev = (uint32_t *)malloc(sizeof(uint32_t) * ((size_t)readLen + (size_t)refLen + 4));
+  int nrev = 0;
+  int i = readLen - 1, j = refLen - 1, cnt = 0, state = 2;
+  char op = 'M', prev = 'M';
+  int ok = 1;
+  while (i > 0) {
+    const int x0 = i - bw > 0 ? i - bw : 0;
+    const int8_t code = dir[(size_t)width_d * 3 * i + (size_t)(j - x0) * 3 + state];
+    switch (code) {
+      case 1: --i; --j; state = 2; op = 'M'; break;
+      case 2: --i; state = 0; op = 'I'; break;
+      case 3: --i; state = 2; op = 'I'; break;
+      case 4: --j; state = 1; op = 'D'; break;
+      case 5: --j; state = 2; op = 'D'; break;
+      default: ok = 0; break;
+    }
+    if (!ok) break;
+    if (op == prev) {
+      ++cnt;
+    } else {
+      rev[nrev++] = ((uint32_t)cnt << 4) | (uint32_t)(prev == 'M' ? SWO_OP_M : prev == 'I' ? SWO_OP_I : SWO_OP_D);
+      prev = op;
+      cnt = 1;
+    }
+  }
+  int n = -1;
+  if (ok) {
+    if (op == 'M') {
+      rev[nrev++] = ((uint32_t)(cnt + 1) << 4) | SWO_OP_M;
+    } else {
+      rev[nrev++] = ((uint32_t)cnt << 4) | (uint32_t)(op == 'I' ? SWO_OP_I : SWO_OP_D);
+      rev[nrev++] = (1u << 4) | SWO_OP_M;
+    }
+    if (nrev <= cap) {
+      for (int k = 0; k < nrev; k++) raw[k] = rev[nrev - 1 - k];
+      n = nrev;
+    }
+  }
+  free(rev);
+  free(hb);
+  free(eb);
+  free(hc);
+  free(dir);
+  return n;
+}
+
+/* Final CIGAR and mismatch count of an alignment res5 = (score, a_begin, a_end, b_begin,
+ * b_end) of A (SSW ref, M codes) and B (SSW query, N codes).  Returns the op count
+ * (0: no CIGAR, score 0) or -1 when cap is too small. */
+int sw_oracle_cigar(const uint8_t *A, int M, const uint8_t *B, int N, const int8_t *mat, int gO, int gE,
+                    const int32_t *res5, uint32_t *ops, int cap, int32_t *mismatches) {
+  *mismatches = 0;
+  const int S = res5[0], ab = res5[1], ae = res5[2], bb = res5[3], be = res5[4];
+  /* no CIGAR for score 0 (SSW then compares a base before its ref, out of bounds) nor past
+   * SSW's distance filter 32767 (ssw_core.cpp:1180) */
+  if (S <= 0 || M <= 0 || N <= 0 || ae - ab > 32767 || be - bb > 32767) return 0;
+  uint32_t *raw = (uint32_t *)malloc(sizeof(uint32_t) * ((size_t)M + (size_t)N + 8));
+  const int nraw = swo_banded(A + ab, ae - ab + 1, B + bb, be - bb + 1, S, mat, gO, gE, raw, M + N + 8);
+  if (nraw < 0) {
+    free(raw);
+    return -1;
+  }
+  int n = 0, mm = 0;
+  const uint8_t *r = A + ab, *q = B + bb;
+  if (bb > 0 && swo_push(ops, cap, &n, (uint32_t)bb, SWO_OP_S)) goto full;
+  for (int k = 0; k < nraw; k++) {
+    const int op = (int)(raw[k] & 0xfu);
+    const uint32_t len = raw[k] >> 4;
+    if (op == SWO_OP_M) {
+      int run_op = -1;
+      uint32_t run = 0;
+      for (uint32_t t = 0; t < len; t++) {
+        const int o = (*r != *q) ? SWO_OP_X : SWO_OP_EQ;
+        if (o == SWO_OP_X) ++mm;
+        if (o != run_op && run > 0) {
+          if (swo_push(ops, cap, &n, run, run_op)) goto full;
+          run = 0;
+        }
+        run_op = o;
+        ++run;
+        ++r;
+        ++q;
+      }
+      if (run > 0 && swo_push(ops, cap, &n, run, run_op)) goto full;
+    } else if (op == SWO_OP_I) {
+      q += len;
+      mm += (int)len;
+      if (swo_push(ops, cap, &n, len, op)) goto full;
+    } else {
+      r += len;
+      mm += (int)len;
+      if (swo_push(ops, cap, &n, len, op)) goto full;
+    }
+  }
+  if (N - be - 1 > 0 && swo_push(ops, cap, &n, (uint32_t)(N - be - 1), SWO_OP_S)) goto full;
+  free(raw);
+  *mismatches = mm;
+  return n;
+full:
+  free(raw);
+  return -1;
+}
+
+/* As sw_oracle_align_batch with a CIGAR per pair (Filter(true, true, 0, 32767)):
+ * out = n*6 int32 (score, a_begin, a_end, b_begin, b_end, mismatches), ops = n*ops_cap
+ * BAM-encoded ops, nops[p] = op count of pair p (0: none, -1: more than ops_cap). */
+int sw_oracle_cigar_batch(const char *a_seqs, const int64_t *a_off, const int32_t *a_len, const char *b_seqs,
+                          const int64_t *b_off, const int32_t *b_len, int64_t n, int match, int mismatch, int gap_open,
+                          int gap_extend, int ambiguity, int nthreads, int32_t *out, uint32_t *ops, int32_t *nops,
+                          int ops_cap) {
+  return swo_batch_run(a_seqs, a_off, a_len, b_seqs, b_off, b_len, n, match, mismatch, gap_open, gap_extend, ambiguity,
+                       nthreads, out, 6, ops, nops, ops_cap);
 }

@@ -16,7 +16,9 @@ $MHSW_REFERENCE) on x86_64; the GPU machine needs only the committed JSON files.
       reference SSW's (score, a_begin, a_end, b_begin, b_end) under those four scorings.
   Both files also record, per scoring, the reference's second-best score and its row
   ("reference_next_best": sw_score_next_best, ref_end_next_best) for maskLen =
-  max(len(A)/2, 15) as klign passes it.
+  max(len(A)/2, 15) as klign passes it, and what the reference returns with
+  report_cigar (Filter(true, true, 0, 32767), the filter klign's post-assembly alignment
+  uses): "reference_cigar" = [cigar_string, mismatches].
 """
 from __future__ import annotations
 
@@ -98,6 +100,12 @@ def parse_adept_test(text: str) -> list[dict]:
     return out
 
 
+def _cigars(oracle, pairs, sc) -> list[list]:
+    out, ops, nops = oracle.ref_cigar_batch(pairs, sc, 1, ops_cap=1024)
+    assert (nops >= 0).all()
+    return [[oracle.cigar_string(ops[i], int(nops[i])), int(out[i, 5])] for i in range(pairs.n)]
+
+
 def main() -> None:
     from mhm2_staging_gb300 import Pairs, workloads
     from oracle import oracle
@@ -115,6 +123,8 @@ def main() -> None:
         for c, o in zip(cases, out.tolist()):
             c.setdefault("reference", {})[name] = o[:5]
             c.setdefault("reference_next_best", {})[name] = o[5:7]
+        for c, cg in zip(cases, _cigars(oracle, pairs, sc)):
+            c.setdefault("reference_cigar", {})[name] = cg
     for c, a in zip(cases, adept):
         assert (c["query"], c["ref"]) == (a["query"], a["ref"])
         c["adept_expect"] = {"qbegin": a["qstart"], "qend": a["qend"], "rbegin": a["rstart"], "rend": a["rend"]}
@@ -138,12 +148,15 @@ def main() -> None:
     ]
     samples += edge
     sp = Pairs.from_lists([s[1] for s in samples], [s[2] for s in samples])
-    rec = [{"set": s[0], "a": s[1], "b": s[2], "reference": {}, "reference_next_best": {}} for s in samples]
+    rec = [{"set": s[0], "a": s[1], "b": s[2], "reference": {}, "reference_next_best": {}, "reference_cigar": {}}
+           for s in samples]
     for name, sc in SCORINGS.items():
         out = oracle.ref_align_batch(sp, sc, 1, score2=True)
         for r, o in zip(rec, out.tolist()):
             r["reference"][name] = o[:5]
             r["reference_next_best"][name] = o[5:7]
+        for r, cg in zip(rec, _cigars(oracle, sp, sc)):
+            r["reference_cigar"][name] = cg
     (HERE / "ssw_reference_samples.json").write_text(json.dumps(
         {"source": "reference SSW (src/ssw/ssw.cpp + ssw_core.cpp) called as klign calls it (src/klign.cpp:257)",
          "orientation": "a = SSW ref (klign: the read), b = SSW query (klign: the contig window)",

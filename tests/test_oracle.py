@@ -138,3 +138,116 @@ def test_second_best_vs_live_reference():
             want = oracle.ref_align_batch(p, sc, score2=True)
             bad = np.nonzero((got != want).any(axis=1))[0]
             assert len(bad) == 0, (cfg, sc, got[bad[:2]].tolist(), want[bad[:2]].tolist())
+
+
+# ---- CIGARs (report_cigar) ------------------------------------------------------------
+
+def _cigar_rows(pairs, sc):
+    out, ops, nops = oracle.cigar_batch(pairs, sc, ops_cap=1024)
+    assert (nops >= 0).all()
+    return out, [oracle.cigar_string(ops[i], int(nops[i])) for i in range(pairs.n)]
+
+
+@pytest.mark.parametrize("scoring", TEST_SCORINGS)
+def test_cigar_known_answers_of_reference_test(scoring):
+    """test/ssw-test.cpp:159-236: the CIGAR strings and mismatch counts the reference's own
+    unit test expects with ssw_filter_cigar (e.g. 8=1X7=, 8=1I8=, 4=1D11=, 3S16=)."""
+    cases, pairs = _kat_pairs()
+    out, cig = _cigar_rows(pairs, tuple(KAT["scorings"][scoring]))
+    n_checked = 0
+    for c, o, s in zip(cases, out.tolist(), cig):
+        if c["kind"] == "aln":
+            assert (s, o[5]) == (c["cigar"], c["mismatches"]), (c["query"], c["ref"], s, o)
+            n_checked += 1
+    assert n_checked == 17
+
+
+@pytest.mark.parametrize("scoring", list(SAMPLES["scorings"]))
+def test_cigar_vs_recorded_reference(scoring):
+    """CIGAR strings and mismatches against the reference's recorded report_cigar output.
+    Score-0 pairs are left out: there SSW's CalculateNumberMismatch reads the base before
+    its reference buffer (ref += ref_begin = -1), so its output is not defined; the oracle
+    returns no CIGAR for them."""
+    recs = SAMPLES["pairs"]
+    pairs = Pairs.from_lists([r["a"] for r in recs], [r["b"] for r in recs])
+    out, cig = _cigar_rows(pairs, tuple(SAMPLES["scorings"][scoring]))
+    n = 0
+    for r, o, s in zip(recs, out.tolist(), cig):
+        if r["reference"][scoring][0] == 0:
+            assert s == "" and o[5] == 0
+            continue
+        assert [s, o[5]] == r["reference_cigar"][scoring], (r["set"], r["a"], r["b"], s, o)
+        n += 1
+    assert n >= 190
+    cases, kp = _kat_pairs()
+    kout, kcig = _cigar_rows(kp, tuple(KAT["scorings"][scoring]))
+    for c, o, s in zip(cases, kout.tolist(), kcig):
+        if c["reference"][scoring][0] > 0:
+            assert [s, o[5]] == c["reference_cigar"][scoring], c
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference SSW not built (needs the reference checkout)")
+def test_cigar_vs_live_reference():
+    """Generated workloads plus indel-heavy, N-rich and unrelated pairs (bands that must
+    double, boxes much longer than wide) against the live reference with report_cigar."""
+    from mhm2_staging_gb300 import workloads
+
+    rng = random.Random(11)
+    a, b = [], []
+    for k in range(3000):
+        x = "".join(rng.choice("ACGT") for _ in range(rng.randint(1, 260)))
+        if k % 4 == 0:
+            y = "".join(rng.choice("ACGTN") for _ in range(rng.randint(1, 300)))
+        else:
+            y = []
+            ind = (0.02, 0.12, 0.3)[k % 3]
+            for ch in x:
+                r = rng.random()
+                if r < ind / 2:
+                    continue
+                if r < ind:
+                    y.append("".join(rng.choice("ACGT") for _ in range(rng.randint(1, 6))))
+                y.append(ch if rng.random() > 0.04 else rng.choice("ACGTN"))
+            y = "".join(rng.choice("ACGT") for _ in range(rng.randint(0, 40))) + "".join(y) + "A"
+        a.append(x)
+        b.append(y)
+    sets = [Pairs.from_lists(a, b)] + [workloads.generate(cfg, n=n, first=77)
+                                       for cfg, n in ((0, 1500), (1, 1500), (2, 1500), (4, 60))]
+    for pairs in sets:
+        for sc in [(1, 3, 5, 2, 2), (2, 4, 4, 2, 1), (2, 2, 3, 1, 2)]:
+            got = oracle.cigar_batch(pairs, sc, ops_cap=1024)
+            want = oracle.ref_cigar_batch(pairs, sc, ops_cap=1024)
+            live = want[0][:, 0] > 0
+            assert np.array_equal(got[0][live], want[0][live]), sc
+            assert np.array_equal(got[2][live], want[2][live]), sc
+            for i in np.nonzero(live)[0]:
+                k = int(got[2][i])
+                assert np.array_equal(got[1][i, :k], want[1][i, :k]), (sc, i)
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference SSW not built (needs the reference checkout)")
+def test_equal_gap_penalties_are_outside_the_contract():
+    """With gap open == gap extend SSW's striped lazy-F loop stops early and can report a
+    score below the local-alignment optimum; the oracle computes the optimum.  klign's
+    scorings all open gaps dearer than they extend them (5/2 and 4/2), where the two
+    agree (the tests above); this records the boundary."""
+    rng = random.Random(3)
+    a, b = [], []
+    for _ in range(3000):  # indel-heavy reads: scores on SSW's word path, long gaps
+        x = "".join(rng.choice("ACGT") for _ in range(rng.randint(150, 300)))
+        y = []
+        for ch in x:
+            r = rng.random()
+            if r < 0.125:
+                continue
+            if r < 0.25:
+                y.append("".join(rng.choice("ACGT") for _ in range(rng.randint(1, 8))))
+            y.append(ch if rng.random() > 0.02 else rng.choice("ACGT"))
+        a.append(x)
+        b.append("".join(y))
+    pairs = Pairs.from_lists(a, b)
+    got = oracle.align_batch(pairs, (2, 2, 2, 2, 2))
+    want = oracle.ref_align_batch(pairs, (2, 2, 2, 2, 2))
+    assert (got[:, 0] >= want[:, 0]).all()
+    assert (got[:, 0] > want[:, 0]).any()
+    assert np.array_equal(oracle.align_batch(pairs, (2, 2, 3, 2, 2)), oracle.ref_align_batch(pairs, (2, 2, 3, 2, 2)))
