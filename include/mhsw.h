@@ -80,6 +80,10 @@ typedef struct {
   int64_t graph_replays; /* CUDA graph launches by this handle so far: a device-resident batch
                           * aligned again with the same pointers, sizes and settings is
                           * captured on its second call and replayed from then on */
+  double cigar_ms;          /* CIGAR mode: the CIGAR pass (device kernels plus the host-driven
+                             * rounds for wide bands), 0 otherwise */
+  int64_t n_cigar_generic;  /* CIGAR mode: pairs whose band or box exceeded the register
+                             * kernels and took the generic kernel */
 } mhsw_timing;
 
 typedef struct {
@@ -161,6 +165,31 @@ int mhsw_driver_set_score2(mhsw_driver *drv, int on);
 /* Second-best scores of the last batch aligned in score2 mode: score2[i] and its A row
  * a_end2[i] (0 and 0 when no row qualifies), host or device pointers as host_io says. */
 int mhsw_last_score2(mhsw_driver *drv, int32_t *score2, int32_t *a_end2, int host_io);
+
+/* CIGAR mode (default off).  klign's post-assembly alignment asks SSW for CIGARs
+ * (ssw_filter.report_cigar, src/klign.cpp:435; Filter(true, true, 0, 32767)) and writes
+ * cigar_string and mismatches into the SAM record (src/klign.cpp:257-271, :178-205); the
+ * reference GPU driver has none and klign falls back to the CPU aligner whenever CIGARs
+ * are wanted (src/klign.cpp:589-600).  With the mode on, mhsw_align_pairs and the
+ * run_kernel_backwards / kernel_block round also compute, per pair, exactly what
+ * StripedSmithWaterman::Aligner::Align returns with report_cigar: banded_sw's traceback
+ * (src/ssw/ssw_core.cpp:854-1053) with the soft clips of ConvertAlignment and the =/X
+ * split and mismatch count of CalculateNumberMismatch (src/ssw/ssw.cpp:57-254).  No CIGAR
+ * (0 ops) for score 0 -- SSW then compares a base outside its reference buffer -- or when
+ * a span exceeds SSW's distance filter of 32767.  Results: mhsw_last_cigar. */
+int mhsw_driver_set_cigar(mhsw_driver *drv, int on);
+/* CIGARs of the last batch aligned in CIGAR mode, in pair order: nops[i] ops (0: none;
+ * -1: not computed, the box or band beyond the kernels' scratch) of pair i at
+ * ops[op_off[i] .. op_off[i] + nops[i]), BAM-encoded (length << 4 | op, op 0..8 of
+ * "MIDNSHP=X"); op_off has n + 1 entries (op_off[n] = total); mismatches[i] as SSW's
+ * Alignment::mismatches.  Any output may be NULL; *ops_total receives the total op count.
+ * ops_cap < total with ops non-NULL fails with MHSW_ERR_ARG (after filling the rest), so
+ * a first call with ops = NULL sizes the buffer.  host_io as in mhsw_last_score2. */
+int mhsw_last_cigar(mhsw_driver *drv, int32_t *nops, int32_t *mismatches, int64_t *op_off, uint32_t *ops,
+                    int64_t ops_cap, int64_t *ops_total, int host_io);
+/* SAM text of nops BAM-encoded ops (Alignment::cigar_string): returns its length, or -1
+ * when buf (cap bytes, NUL included) is too small. */
+int64_t mhsw_cigar_format(const uint32_t *ops, int32_t nops, char *buf, int64_t cap);
 
 /* GPUDriver::run_kernel_forwards (driver.cpp:281-375): copies the batch, launches
  * the forward pass and the copy of the end coordinates and scores; returns without

@@ -112,6 +112,23 @@ struct mhsw_driver {
   DBuf<int32_t> rowmax16, rowmax8, r_score2, r_aend2;
   HBuf<int32_t> h_score2;  // drop-in protocol: score2 then a_end2, n each
   mhsw::Forks forks;          // side streams for launches that overlap on the device
+  // CIGAR mode: SSW's report_cigar output per pair (ops arena, lists, scratch)
+  bool cigar = false;
+  int64_t cigar_n = -1;        // pairs of the last batch whose CIGARs are in the arena
+  int64_t cigar_total = -1;    // ops in pair order (after the ordered copy), -1 before it
+  double cigar_ms = 0;
+  int64_t cigar_generic = 0;   // pairs of the last batch that took the generic kernel
+  int sms = 152;
+  DBuf<int32_t> c_nops, c_mism;
+  DBuf<int64_t> c_off, c_ordoff, c_c64;
+  DBuf<uint32_t> c_arena, c_ordops, c_dirs;
+  DBuf<unsigned long long> c_cursor;
+  DBuf<int> c_counts;
+  DBuf<int2> c_lists;
+  DBuf<int4> c_generic, c_gsorted;
+  DBuf<unsigned char> c_pool, c_temp;
+  HBuf<int> h_ccounts;
+  cudaEvent_t ev_c[2] = {nullptr, nullptr};
 
   // CUDA graph of a device-resident batch: captured the second time the same batch
   // (same pointers, sizes and settings) is aligned, replayed from then on.
@@ -119,7 +136,7 @@ struct mhsw_driver {
     const void *ptr[7];
     int64_t n, a_bytes, b_bytes;
     int32_t max_a, max_b;
-    int form, ceiling, match, mismatch, gap_open, gap_extend, ambiguity, score2;
+    int form, ceiling, match, mismatch, gap_open, gap_extend, ambiguity, score2, cigar;
     bool operator==(const GraphKey &o) const { return std::memcmp(this, &o, sizeof(GraphKey)) == 0; }
   };
   GraphKey gkey{};
@@ -191,6 +208,24 @@ struct mhsw_driver {
     r_score2.release();
     r_aend2.release();
     h_score2.release();
+    c_nops.release();
+    c_mism.release();
+    c_off.release();
+    c_ordoff.release();
+    c_c64.release();
+    c_arena.release();
+    c_ordops.release();
+    c_dirs.release();
+    c_cursor.release();
+    c_counts.release();
+    c_lists.release();
+    c_generic.release();
+    c_gsorted.release();
+    c_pool.release();
+    c_temp.release();
+    h_ccounts.release();
+    for (auto &e : ev_c)
+      if (e) cudaEventDestroy(e);
     h_a.release();
     h_b.release();
     h_aoff.release();
@@ -267,6 +302,128 @@ int attach_score2(mhsw_driver *d, mhsw::PairSet *ps, int64_t n, int64_t a_bytes)
   MHSW_CK(d->r_aend2.reserve((size_t)n + 1), "cudaMalloc results");
   ps->rowmax16 = d->rowmax16.p;
   ps->rowmax8 = d->rowmax8.p;
+  return MHSW_OK;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();  // not sticky: keep it from surfacing as a later call's error
+    return 0.f;
+  }
+  return ms;
+}
+
+// ---- CIGAR mode ------------------------------------------------------------------
+
+int ensure_cigar(mhsw_driver *d, int64_t n) {
+  MHSW_CK(d->c_nops.reserve((size_t)n + 1), "cudaMalloc CIGAR");
+  MHSW_CK(d->c_mism.reserve((size_t)n + 1), "cudaMalloc CIGAR");
+  MHSW_CK(d->c_off.reserve((size_t)n + 1), "cudaMalloc CIGAR");
+  MHSW_CK(d->c_lists.reserve((size_t)mhsw::kCigarClasses * ((size_t)n + 1)), "cudaMalloc CIGAR lists");
+  MHSW_CK(d->c_generic.reserve((size_t)n + 1), "cudaMalloc CIGAR lists");
+  MHSW_CK(d->c_counts.reserve(mhsw::kCigarCounters), "cudaMalloc CIGAR");
+  MHSW_CK(d->c_cursor.reserve(1), "cudaMalloc CIGAR");
+  MHSW_CK(d->c_dirs.reserve(mhsw::kCigarDirBudget / sizeof(uint32_t)), "cudaMalloc CIGAR scratch");
+  // 32 ops per pair on average before the arena has to grow (finish_cigar grows it)
+  MHSW_CK(d->c_arena.reserve(std::max<size_t>((size_t)n * 32, 1 << 16)), "cudaMalloc CIGAR arena");
+  MHSW_CK(d->h_ccounts.reserve(mhsw::kCigarCounters + 2), "cudaMallocHost");
+  return MHSW_OK;
+}
+
+mhsw::CigarBufs cigar_bufs(mhsw_driver *d, int64_t n) {
+  mhsw::CigarBufs cb;
+  cb.nops = d->c_nops.p;
+  cb.mism = d->c_mism.p;
+  cb.op_off = d->c_off.p;
+  cb.arena = d->c_arena.p;
+  cb.arena_cap = (int64_t)d->c_arena.cap;
+  cb.cursor = d->c_cursor.p;
+  cb.counts = d->c_counts.p;
+  cb.lists = d->c_lists.p;
+  cb.list_cap = n + 1;
+  cb.generic = d->c_generic.p;
+  cb.dirs = d->c_dirs.p;
+  cb.dirs_bytes = d->c_dirs.cap * sizeof(uint32_t);
+  return cb;
+}
+
+// Classification and the register-band kernels, then the counters' copy to the host
+// (all stream-ordered; part of a captured graph when the batch is captured).
+int enqueue_cigar(mhsw_driver *d, const mhsw::PairSet &ps) {
+  MHSW_CK(mhsw::launch_cigar(ps, result_set(d), d->sc, cigar_bufs(d, ps.n), d->sms, d->st, &d->launches),
+          "CIGAR launch");
+  MHSW_CK(cudaMemcpyAsync(d->h_ccounts.p, d->c_counts.p, sizeof(int) * mhsw::kCigarCounters, cudaMemcpyDeviceToHost,
+                          d->st),
+          "D2H CIGAR counters");
+  return MHSW_OK;
+}
+
+// After the batch's stream work completed: grows the arena and runs the pass again when
+// it filled up, and runs the generic kernel over the pairs the register kernels left
+// (bands wider than 31 or boxes longer than kCigarRowCap rows), in rounds sized to a
+// scratch budget.  Synchronous; rare work outside the captured graph.
+int finish_cigar(mhsw_driver *d, const mhsw::PairSet &ps) {
+  const int64_t n = ps.n;
+  const auto t0 = std::chrono::steady_clock::now();
+  d->cigar_generic = 0;
+  bool generic_done = false;
+  for (int round = 0; round < 4; round++) {
+    const int *cnt = d->h_ccounts.p;
+    if (cnt[mhsw::kCigarClasses + 1] > 0) {  // arena full: grow to what was asked for, run again
+      unsigned long long need = 0;
+      MHSW_CK(cudaMemcpy(&need, d->c_cursor.p, sizeof(need), cudaMemcpyDeviceToHost), "D2H cursor");
+      MHSW_CK(d->c_arena.reserve((size_t)need + (size_t)n * 8 + 1024), "cudaMalloc CIGAR arena");
+      int rc = enqueue_cigar(d, ps);
+      if (rc) return rc;
+      MHSW_CK(cudaStreamSynchronize(d->st), "sync");
+      generic_done = false;
+      continue;
+    }
+    const int ng = cnt[mhsw::kCigarClasses];
+    if (ng > 0 && !generic_done) {
+      generic_done = true;
+      d->cigar_generic = ng;
+      std::vector<int4> ent((size_t)ng);
+      MHSW_CK(cudaMemcpy(ent.data(), d->c_generic.p, sizeof(int4) * ng, cudaMemcpyDeviceToHost), "D2H generic list");
+      // the widest band a box can need: doubling from w stops once it covers the box
+      auto slice_of = [](const int4 &e) {
+        int w = e.y;
+        while (w < std::max(e.z, e.w)) w *= 2;
+        return (mhsw::cigar_slice_bytes(w, e.z) + 15) / 16 * 16;
+      };
+      std::sort(ent.begin(), ent.end(), [&](const int4 &a, const int4 &b) { return slice_of(a) > slice_of(b); });
+      MHSW_CK(d->c_gsorted.reserve((size_t)ng), "cudaMalloc generic list");
+      MHSW_CK(cudaMemcpy(d->c_gsorted.p, ent.data(), sizeof(int4) * ng, cudaMemcpyHostToDevice), "H2D generic list");
+      const size_t budget = size_t(1) << 30;
+      size_t at = 0;
+      while (at < (size_t)ng) {
+        const size_t slice = slice_of(ent[at]);
+        size_t end = at + 1;
+        while (end < (size_t)ng && slice_of(ent[end]) * 2 > slice) end++;  // same size class
+        const size_t pool = std::max(budget, slice);
+        const int threads = (int)std::max<size_t>(1, std::min<size_t>({end - at, pool / slice, 8192}));
+        MHSW_CK(d->c_pool.reserve(slice * (size_t)threads), "cudaMalloc CIGAR pool");
+        MHSW_CK(mhsw::launch_cigar_generic(ps, result_set(d), d->sc, cigar_bufs(d, n), d->c_gsorted.p + at,
+                                           (int)(end - at), threads, slice, d->c_pool.p, d->st),
+                "CIGAR generic launch");
+        d->launches += 1;
+        at = end;
+      }
+      MHSW_CK(cudaMemcpyAsync(d->h_ccounts.p, d->c_counts.p, sizeof(int) * mhsw::kCigarCounters,
+                              cudaMemcpyDeviceToHost, d->st),
+              "D2H CIGAR counters");
+      MHSW_CK(cudaStreamSynchronize(d->st), "sync");
+      continue;  // the generic kernel may have found the arena full
+    }
+    break;
+  }
+  if (d->h_ccounts.p[mhsw::kCigarClasses + 1] > 0)
+    return d->fail(MHSW_ERR_INTERNAL, "CIGAR arena still full after growing it");
+  d->cigar_n = n;
+  d->cigar_total = -1;
+  d->cigar_ms = elapsed(d->ev_c[0], d->ev_c[1]) +
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return MHSW_OK;
 }
 
@@ -528,15 +685,6 @@ int ready(mhsw_driver *d) {
   return MHSW_OK;
 }
 
-float elapsed(cudaEvent_t a, cudaEvent_t b) {
-  float ms = 0.f;
-  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
-    cudaGetLastError();  // not sticky: keep it from surfacing as a later call's error
-    return 0.f;
-  }
-  return ms;
-}
-
 }  // namespace
 
 extern "C" {
@@ -642,6 +790,8 @@ int mhsw_driver_init(mhsw_driver *d, int rank_me, int rank_n, short match_score,
   MHSW_CK(cudaEventCreateWithFlags(&d->ev_done, cudaEventDisableTiming), "cudaEventCreate");
   MHSW_CK(mhsw::forks_create(d->forks), "side streams");
   for (auto &e : d->ev_t) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
+  for (auto &e : d->ev_c) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
+  MHSW_CK(cudaDeviceGetAttribute(&d->sms, cudaDevAttrMultiProcessorCount, d->device), "device attribute");
   d->sc = s;
   d->inited = true;
   // Pre-size for a reference-sized block (KLIGN_GPU_BLOCK_SIZE = 20000 pairs).
@@ -721,6 +871,7 @@ int mhsw_run_kernel_forwards(mhsw_driver *d, const char *const *reads, const int
   d->ev_live = false;
   d->fwd_issued = d->rev_issued = false;
   d->launches = 0;
+  d->cigar_n = -1;
   MHSW_CK(cudaEventRecord(d->ev_t[0], d->st), "event");
   rc = stage_strings(d, reads, read_lens, contigs, contig_lens, n);
   if (rc) return rc;
@@ -784,9 +935,18 @@ int mhsw_run_kernel_backwards(mhsw_driver *d, const char *const *reads, const in
     return d->fail(MHSW_ERR_ARG, "batch size %d differs from the forward batch (%lld)", n, (long long)d->n_batch);
   mhsw::PairSet ps = staged_pairs(d);
   MHSW_CK(cudaEventRecord(d->ev_t[4], d->st), "event");
+  d->cigar_n = -1;
   if (n > 0) {
     rc = run_reverse(d, ps, d->max_a, d->max_b, d->fwd_order);
     if (rc) return rc;
+    if (d->cigar) {
+      rc = ensure_cigar(d, n);
+      if (rc) return rc;
+      MHSW_CK(cudaEventRecord(d->ev_c[0], d->st), "event");
+      rc = enqueue_cigar(d, ps);
+      if (rc) return rc;
+      MHSW_CK(cudaEventRecord(d->ev_c[1], d->st), "event");
+    }
   }
   mhsw::OutViews dv, hv;
   rc = ensure_outviews(d, std::max<int64_t>(n, 1), &dv, &hv);
@@ -836,6 +996,10 @@ int mhsw_kernel_block(mhsw_driver *d) {
   std::lock_guard<std::mutex> lk(d->mu);
   if (!d->ev_live) return MHSW_OK;
   MHSW_CK(cudaEventSynchronize(d->ev_done), "cudaEventSynchronize");
+  if (d->rev_issued && d->cigar && d->n_batch > 0 && d->cigar_n < 0) {
+    const int rc = finish_cigar(d, staged_pairs(d));
+    if (rc) return rc;
+  }
   if (d->rev_issued && d->n_batch > 0 && d->h_counts.p) {
     // timing of the completed protocol round
     d->timing.fwd_ms = elapsed(d->ev_t[1], d->ev_t[2]);
@@ -982,6 +1146,11 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
   }
   rc = attach_score2(d, &ps, n, ta);
   if (rc) return rc;
+  d->cigar_n = -1;
+  if (d->cigar && n > 0) {
+    rc = ensure_cigar(d, n);
+    if (rc) return rc;
+  }
   // Everything from translation to the result copy, on the handle's stream.
   // Phase events recorded inside a capture become external event nodes, so a replayed
   // graph still records them and the phase timings stay available.
@@ -1005,6 +1174,12 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
       if (r) return r;
     }
     MHSW_CK(mark(d->ev_t[3]), "event");
+    if (n > 0 && d->cigar) {
+      MHSW_CK(mark(d->ev_c[0]), "event");
+      int r = enqueue_cigar(d, ps);
+      if (r) return r;
+      MHSW_CK(mark(d->ev_c[1]), "event");
+    }
     if (n > 0) {
       if (host_io) {
         MHSW_CK(mhsw::launch_pack5(result_set(d), n, d->out5.p, d->st), "pack5");
@@ -1038,6 +1213,7 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
     key.gap_extend = d->sc.gap_extend;
     key.ambiguity = d->sc.ambiguity;
     key.score2 = d->score2 ? 1 : 0;
+    key.cigar = d->cigar ? 1 : 0;
   }
   const bool same = hinted && d->use_graphs && n > 0 && d->gkey_seen && key == d->gkey;
   if (same && d->gexec) {
@@ -1092,6 +1268,12 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
   MHSW_CK(cudaEventSynchronize(d->ev_t[4]), "sync");
   // Surface any asynchronous kernel fault as an error status.
   MHSW_CK(cudaGetLastError(), "kernel execution");
+  d->cigar_ms = 0;
+  d->cigar_generic = 0;
+  if (n > 0 && d->cigar) {
+    rc = finish_cigar(d, ps);
+    if (rc) return rc;
+  }
   d->timing.fwd_ms = elapsed(d->ev_t[1], d->ev_t[2]);
   d->timing.rev_ms = elapsed(d->ev_t[2], d->ev_t[3]);
   d->timing.total_ms = elapsed(d->ev_t[0], d->ev_t[4]);
@@ -1101,6 +1283,8 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
   d->timing.n_rev_wide = n > 0 ? d->h_counts.p[1] : 0;
   d->timing.launches = d->launches;
   d->timing.graph_replays = d->graph_launches;
+  d->timing.cigar_ms = d->cigar_ms;
+  d->timing.n_cigar_generic = d->cigar_generic;
   return MHSW_OK;
 }
 
@@ -1131,6 +1315,84 @@ int mhsw_last_score2(mhsw_driver *d, int32_t *score2, int32_t *a_end2, int host_
   MHSW_CK(cudaMemcpyAsync(a_end2, d->r_aend2.p, sizeof(int32_t) * n, k, d->st), "copy score2");
   MHSW_CK(cudaStreamSynchronize(d->st), "sync");
   return MHSW_OK;
+}
+
+int mhsw_driver_set_cigar(mhsw_driver *d, int on) {
+  if (!d) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  d->cigar = on != 0;
+  return MHSW_OK;
+}
+
+int mhsw_last_cigar(mhsw_driver *d, int32_t *nops, int32_t *mismatches, int64_t *op_off, uint32_t *ops,
+                    int64_t ops_cap, int64_t *ops_total, int host_io) {
+  int rc = ready(d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(d->mu);
+  const int64_t n = d->cigar_n;
+  if (n < 0) return d->fail(MHSW_ERR_STATE, "no CIGARs: CIGAR mode was off for the last batch, or it has not completed");
+  if (n == 0) {
+    if (ops_total) *ops_total = 0;
+    if (op_off) {
+      const int64_t z = 0;
+      MHSW_CK(cudaMemcpy(op_off, &z, sizeof(z), host_io ? cudaMemcpyHostToHost : cudaMemcpyHostToDevice), "copy");
+    }
+    return MHSW_OK;
+  }
+  if (d->cigar_total < 0) {  // pair-order copy of the arena, once per batch
+    size_t temp = 0;
+    MHSW_CK(mhsw::cigar_gather_temp_bytes(n, &temp), "scan size");
+    MHSW_CK(d->c_temp.reserve(temp + 16), "cudaMalloc scan");
+    MHSW_CK(d->c_c64.reserve((size_t)n + 1), "cudaMalloc CIGAR");
+    MHSW_CK(d->c_ordoff.reserve((size_t)n + 1), "cudaMalloc CIGAR");
+    unsigned long long used = 0;
+    MHSW_CK(cudaMemcpy(&used, d->c_cursor.p, sizeof(used), cudaMemcpyDeviceToHost), "D2H cursor");
+    MHSW_CK(d->c_ordops.reserve((size_t)used + 1), "cudaMalloc CIGAR");
+    MHSW_CK(mhsw::launch_cigar_gather(cigar_bufs(d, n), n, d->c_c64.p, d->c_ordoff.p, d->c_ordops.p, d->c_temp.p,
+                                      d->c_temp.cap, d->st),
+            "CIGAR gather");
+    int64_t total = 0;
+    MHSW_CK(cudaMemcpyAsync(&total, d->c_ordoff.p + n, sizeof(total), cudaMemcpyDeviceToHost, d->st), "D2H total");
+    MHSW_CK(cudaStreamSynchronize(d->st), "sync");
+    d->cigar_total = total;
+  }
+  if (ops_total) *ops_total = d->cigar_total;
+  const cudaMemcpyKind k = host_io ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  if (nops) MHSW_CK(cudaMemcpyAsync(nops, d->c_nops.p, sizeof(int32_t) * n, k, d->st), "copy op counts");
+  if (mismatches) MHSW_CK(cudaMemcpyAsync(mismatches, d->c_mism.p, sizeof(int32_t) * n, k, d->st), "copy mismatches");
+  if (op_off) MHSW_CK(cudaMemcpyAsync(op_off, d->c_ordoff.p, sizeof(int64_t) * (n + 1), k, d->st), "copy offsets");
+  if (ops) {
+    if (ops_cap < d->cigar_total) {
+      cudaStreamSynchronize(d->st);
+      return d->fail(MHSW_ERR_ARG, "ops buffer holds %lld ops, the batch has %lld", (long long)ops_cap,
+                     (long long)d->cigar_total);
+    }
+    if (d->cigar_total > 0)
+      MHSW_CK(cudaMemcpyAsync(ops, d->c_ordops.p, sizeof(uint32_t) * d->cigar_total, k, d->st), "copy ops");
+  }
+  MHSW_CK(cudaStreamSynchronize(d->st), "sync");
+  return MHSW_OK;
+}
+
+int64_t mhsw_cigar_format(const uint32_t *ops, int32_t nops, char *buf, int64_t cap) {
+  static const char kOps[] = "MIDNSHP=X";
+  if (nops < 0 || (nops > 0 && !ops) || !buf || cap <= 0) return -1;
+  int64_t at = 0;
+  for (int32_t t = 0; t < nops; t++) {
+    const uint32_t c = ops[t], code = c & 15u;
+    char tmp[16];
+    int k = 0;
+    uint32_t len = c >> 4;
+    do {
+      tmp[k++] = (char)('0' + len % 10);
+      len /= 10;
+    } while (len);
+    if (at + k + 1 >= cap) return -1;
+    while (k) buf[at++] = tmp[--k];
+    buf[at++] = code <= 8 ? kOps[code] : '?';
+  }
+  buf[at] = '\0';
+  return at;
 }
 
 }  // extern "C"

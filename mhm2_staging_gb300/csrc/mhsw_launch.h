@@ -106,6 +106,48 @@ cudaError_t launch_finalize(const ResultSet &rs, int64_t n, bool a_is_query, int
 // Packs results into n x 5 int32 rows (score, a_beg, a_end, b_beg, b_end).
 cudaError_t launch_pack5(const ResultSet &rs, int64_t n, int32_t *out5, cudaStream_t st);
 
+// ---- CIGAR pass (mhsw_cigar.cu) ----------------------------------------------------
+constexpr int kCigarClasses = 5;     // register-band traceback kernels, half-widths 1, 3, 7, 15, 31
+constexpr int kCigarRowCap = 512;    // box rows those kernels keep directions for
+// Counters: [0 .. kCigarClasses-1] class list sizes, [kCigarClasses] generic list size,
+// [+1] pairs that found the arena full, [+2] tracebacks that left the computed band.
+constexpr int kCigarCounters = kCigarClasses + 3;
+constexpr size_t kCigarDirBudget = size_t(256) << 20;  // direction scratch of the register kernels
+
+// Generic-kernel slice of one pair at half-width w: H and E rows plus 4-bit directions.
+__host__ __device__ inline size_t cigar_slice_bytes(int w, int rows) {
+  return 4 * (2 * (size_t)(2 * w + 2) + (size_t)rows * (size_t)((2 * w + 1 + 7) / 8));
+}
+
+struct CigarBufs {           // device buffers of the CIGAR pass
+  int32_t *nops, *mism;      // per pair: op count (0 none, -1 not computed) and mismatches
+  int64_t *op_off;           // per pair: first op in the arena
+  uint32_t *arena;           // BAM-encoded ops, in completion order
+  int64_t arena_cap;
+  unsigned long long *cursor;
+  int *counts;               // kCigarCounters
+  int2 *lists;               // kCigarClasses segments of list_cap (pair, half-width) entries
+  int64_t list_cap;
+  int4 *generic;             // generic list: (pair, half-width, rows, columns), list_cap entries
+  uint32_t *dirs;            // direction scratch, dirs_bytes
+  size_t dirs_bytes;
+};
+
+// Classification and the register-band kernels (no host synchronisation).  Pairs left
+// for the generic kernel are in cb.generic (count in cb.counts[kCigarClasses]).
+cudaError_t launch_cigar(const PairSet &ps, const ResultSet &rs, const Scoring &sc, const CigarBufs &cb, int sms,
+                         cudaStream_t st, int64_t *launches);
+// Generic kernel over `count` entries (device copy), `threads` threads with a slice of
+// `slice` bytes each in `pool`.
+cudaError_t launch_cigar_generic(const PairSet &ps, const ResultSet &rs, const Scoring &sc, const CigarBufs &cb,
+                                 const int4 *entries, int count, int threads, size_t slice, void *pool,
+                                 cudaStream_t st);
+// Pair-order copy: ord_off[0..n] = exclusive sum of the op counts, ord_ops = the ops in
+// pair order (ord_ops may be null to get the offsets only).  c64: n + 1 int64 scratch.
+cudaError_t cigar_gather_temp_bytes(int64_t n, size_t *bytes);
+cudaError_t launch_cigar_gather(const CigarBufs &cb, int64_t n, int64_t *c64, int64_t *ord_off, uint32_t *ord_ops,
+                                void *temp, size_t temp_bytes, cudaStream_t st);
+
 int launches_per_batch();
 
 }  // namespace mhsw

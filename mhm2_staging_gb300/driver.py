@@ -57,6 +57,8 @@ class Timing(C.Structure):
         ("n_rev_wide", C.c_int64),
         ("launches", C.c_int64),
         ("graph_replays", C.c_int64),
+        ("cigar_ms", C.c_double),
+        ("n_cigar_generic", C.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -153,6 +155,9 @@ SIGNATURES: dict[str, tuple] = {
     "mhsw_driver_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "mhsw_driver_set_score2": (C.c_int, [_P, C.c_int]),
     "mhsw_last_score2": (C.c_int, [_P, _P, _P, C.c_int]),
+    "mhsw_driver_set_cigar": (C.c_int, [_P, C.c_int]),
+    "mhsw_last_cigar": (C.c_int, [_P, _P, _P, _P, _P, C.c_int64, C.POINTER(C.c_int64), C.c_int]),
+    "mhsw_cigar_format": (C.c_int64, [_P, C.c_int32, C.c_char_p, C.c_int64]),
     "mhsw_run_kernel_forwards": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32, C.c_uint32, C.c_uint32]),
     "mhsw_run_kernel_backwards": (C.c_int, [_P, _P, _P, _P, _P, C.c_int32, C.c_uint32, C.c_uint32]),
     "mhsw_kernel_is_done": (C.c_int, [_P, C.POINTER(C.c_int)]),
@@ -298,6 +303,28 @@ def _as_bytes_list(seqs: Sequence[str | bytes]) -> list[bytes]:
     return [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
 
 
+CIGAR_OPS = "MIDNSHP=X"
+
+
+@dataclass
+class Cigars:
+    """CIGARs of a batch in pair order: pair i has nops[i] BAM-encoded ops (length << 4 |
+    op) at ops[op_off[i] : op_off[i] + nops[i]]; 0 ops: none (score 0, or a span beyond
+    SSW's distance filter); -1: not computed.  mismatches as SSW's Alignment::mismatches."""
+    nops: np.ndarray
+    mismatches: np.ndarray
+    op_off: np.ndarray
+    ops: np.ndarray
+
+    def of(self, i: int) -> np.ndarray:
+        k = max(int(self.nops[i]), 0)
+        return self.ops[self.op_off[i]:self.op_off[i] + k]
+
+    def string(self, i: int) -> str:
+        """SAM CIGAR text of pair i (SSW's cigar_string)."""
+        return "".join(f"{int(c) >> 4}{CIGAR_OPS[int(c) & 15]}" for c in self.of(i))
+
+
 class GPUDriver:
     """Mirror of adept_sw::GPUDriver (reference src/adept-sw/driver.hpp:37-55)."""
 
@@ -348,6 +375,23 @@ class GPUDriver:
         self._ck(self._lib.mhsw_last_score2(self._h, s2.ctypes.data if n else None, a2.ctypes.data if n else None, 1),
                  "last_score2")
         return np.stack([s2, a2], axis=1)
+
+    def set_cigar(self, on: bool) -> None:
+        """CIGAR mode: also compute SSW's report_cigar output (klign's post-assembly SAM)."""
+        self._ck(self._lib.mhsw_driver_set_cigar(self._h, 1 if on else 0), "set_cigar")
+
+    def last_cigar(self, n: int) -> Cigars:
+        """CIGARs of the last batch aligned in CIGAR mode (n pairs), in pair order."""
+        nops = np.zeros(n, dtype=np.int32)
+        mism = np.zeros(n, dtype=np.int32)
+        off = np.zeros(n + 1, dtype=np.int64)
+        total = C.c_int64(0)
+        self._ck(self._lib.mhsw_last_cigar(self._h, nops.ctypes.data if n else None, mism.ctypes.data if n else None,
+                                           off.ctypes.data, None, 0, C.byref(total), 1), "last_cigar")
+        ops = np.zeros(max(int(total.value), 1), dtype=np.uint32)
+        self._ck(self._lib.mhsw_last_cigar(self._h, None, None, None, ops.ctypes.data, ops.shape[0], C.byref(total),
+                                           1), "last_cigar")
+        return Cigars(nops, mism, off, ops[:int(total.value)])
 
     def stream(self) -> int:
         s = _P()

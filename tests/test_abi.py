@@ -63,6 +63,25 @@ def test_host_side_status_codes(lib):
         lib.mhsw_driver_destroy(h)
 
 
+def test_cigar_format_and_state_checks(lib):
+    """mhsw_cigar_format is host code: SAM text of BAM-encoded ops (Alignment::cigar_string)."""
+    ops = (C.c_uint32 * 5)((3 << 4) | 4, (8 << 4) | 7, (1 << 4) | 8, (12 << 4) | 1, (150 << 4) | 2)
+    buf = C.create_string_buffer(64)
+    n = lib.mhsw_cigar_format(ops, 5, buf, 64)
+    assert buf.value == b"3S8=1X12I150D" and n == len(buf.value)
+    assert lib.mhsw_cigar_format(ops, 5, buf, 8) == -1  # too small: refused, nothing claimed
+    assert lib.mhsw_cigar_format(ops, 0, buf, 64) == 0 and buf.value == b""
+    h = C.c_void_p()
+    assert lib.mhsw_driver_create(C.byref(h)) == 0
+    try:
+        assert lib.mhsw_driver_set_cigar(h, 1) == 0
+        total = C.c_int64(0)
+        # not initialised, nothing aligned: a state error (MHSW_ERR_STATE), not a crash
+        assert lib.mhsw_last_cigar(h, None, None, None, None, 0, C.byref(total), 1) == 3
+    finally:
+        lib.mhsw_driver_destroy(h)
+
+
 def test_limits(lib):
     lim = D.Limits()
     assert lib.mhsw_limits(C.byref(lim)) == 0
