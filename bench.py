@@ -223,7 +223,8 @@ def run_paths(drv, dev, torch, stream) -> dict:
     the 150/300 bp batch (plain and batched form), the 1M-pair read/ref mix with 30%
     unrelated reads, the 200k long-reference batch, and the 200k-pair slice of the uneven
     batch with every pair re-run by the int32 engine (int16 ceiling 0), and the same slice in
-    score2 mode (SSW's second-best score as well)."""
+    score2 mode (SSW's second-best score as well) and in CIGAR mode (SSW's report_cigar
+    output as well; beside it the oracle's CIGAR port timed on the host cores on a sample)."""
     from mhm2_staging_gb300 import FORM_BATCHED, FORM_PLAIN, workloads
     from mhm2_staging_gb300.driver import DevicePairs, limits
 
@@ -233,7 +234,8 @@ def run_paths(drv, dev, torch, stream) -> dict:
              ("reads_100_250bp_1M_pairs_30pct_unrelated", 1, 1_000_000, FORM_BATCHED, None),
              ("250bp_vs_2_8kb_refs_200k_pairs", 4, 200_000, FORM_BATCHED, None),
              ("uneven_200k_pairs_all_int32", 2, 200_000, FORM_BATCHED, 0),
-             ("uneven_200k_pairs_score2_mode", 2, 200_000, FORM_BATCHED, "score2")]
+             ("uneven_200k_pairs_score2_mode", 2, 200_000, FORM_BATCHED, "score2"),
+             ("uneven_200k_pairs_cigar_mode", 2, 200_000, FORM_BATCHED, "cigar")]
     default_ceiling = limits().int16_ceiling
     for name, cfg, n, form, ceiling in specs:
         pp = workloads.generate(cfg, n=n)
@@ -244,8 +246,10 @@ def run_paths(drv, dev, torch, stream) -> dict:
                          max_b_len=int(pp.b_len.max()), cells=cells, a_bytes=int((pp.a_off + pp.a_len).max()),
                          b_bytes=int((pp.b_off + pp.b_len).max()))
         score2 = ceiling == "score2"
+        cigar = ceiling == "cigar"
         drv.set_score2(score2)
-        drv.set_int16_ceiling(default_ceiling if ceiling is None or score2 else ceiling)
+        drv.set_cigar(cigar)
+        drv.set_int16_ceiling(default_ceiling if ceiling is None or score2 or cigar else ceiling)
         for _ in range(2):
             drv.align_pairs_device(dp, o.data_ptr(), form=form)
         torch.cuda.synchronize(dev)
@@ -263,11 +267,32 @@ def run_paths(drv, dev, torch, stream) -> dict:
         out[name] = {"gcups": cells / (ms * 1e-3) / 1e9, "ms_per_step": ms, "pairs": pp.n, "cells": cells,
                      "fwd_gcups": cells / (statistics.mean(fwd) * 1e-3) / 1e9,
                      "int32_reruns": int(t["n_overflow16"]), "form": "plain" if form == FORM_PLAIN else "batched"}
+        if cigar:
+            cg = drv.last_cigar(pp.n)
+            out[name].update({"alignments_per_s": pp.n / (ms * 1e-3), "cigar_ms": t["cigar_ms"],
+                              "cigar_generic_pairs": int(t["n_cigar_generic"]),
+                              "cigar_ops": int(cg.op_off[-1]), "cigar_pairs": int((cg.nops > 0).sum())})
+            out[name]["cpu_port"] = _cigar_cpu_port(pp)
         del tens, o
         torch.cuda.empty_cache()
     drv.set_int16_ceiling(default_ceiling)
     drv.set_score2(False)
+    drv.set_cigar(False)
     return out
+
+
+def _cigar_cpu_port(pairs, n: int = 20_000) -> dict:
+    """The oracle's CIGAR port (score, begins and SSW's report_cigar output) on the host
+    cores, on the first n pairs of the same slice."""
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    sub = pairs.slice(0, min(n, pairs.n))
+    t0 = time.perf_counter()
+    oracle.cigar_batch(sub, SCORING, threads, ops_cap=1024)
+    dt = time.perf_counter() - t0
+    return {"alignments_per_s": sub.n / dt, "cores": threads, "kind": "port",
+            "sample": f"first {sub.n} pairs of the slice ({dt:.1f} s)"}
 
 
 def main() -> None:
@@ -283,6 +308,8 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-paths", action="store_true", help="skip the per-workload path measurements")
+    ap.add_argument("--cigar", action="store_true",
+                    help="CIGAR mode in the timed regions (SSW's report_cigar output as well; e2e copies it back)")
     ap.add_argument("--workload", choices=["batch", "serving"], default="batch",
                     help="batch: the uneven-length batch (default); serving: latency under offered load")
     ap.add_argument("--slots", type=int, default=3, help="serving: micro-batches in flight")
@@ -316,6 +343,7 @@ def main() -> None:
     drv = GPUDriver()
     drv.init(local, ws, SCORING[0], -SCORING[1], -SCORING[2], -SCORING[3], 0)
     drv.set_ambiguity(-SCORING[4])
+    drv.set_cigar(args.cigar)
     stream = torch.cuda.ExternalStream(drv.stream(), device=dev)
 
     # resident inputs
@@ -418,7 +446,11 @@ def main() -> None:
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         drv.align_pairs(hp, form=FORM_BATCHED, out=hout, hints=True)
+        if args.cigar:
+            cg = drv.last_cigar(pairs.n)
     e2e_s = allmax((time.perf_counter() - t0) / args.e2e_steps)
+    if args.cigar:
+        d2h += int(cg.nops.nbytes + cg.mismatches.nbytes + cg.op_off.nbytes + cg.ops.nbytes)
     e2e_gcups = cells_all / e2e_s / 1e9
     # the e2e results must equal the resident-input results
     assert np.array_equal(hout, out_dev.cpu().numpy()), "e2e results differ from device-resident results"
@@ -426,6 +458,7 @@ def main() -> None:
     # ---- other paths of the scope: per-workload GCUPS, device-resident ----------------
     paths = None
     if rank == 0 and not args.no_paths:
+        drv.set_cigar(False)
         paths = run_paths(drv, dev, torch, stream)
 
     # ---- roofline of the dominant kernel (the persistent forward kernel) -------------
@@ -469,8 +502,9 @@ def main() -> None:
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int16x2 (int32 re-run on overflow)",
             "data": "synthetic (seeded generator, workload shapes of the reference's measured configs)",
-            "config": {"workload": WORKLOAD_NAME if args.config == 2 and args.pairs is None else
-                       f"config {args.config}, {n_per} pairs per GPU", "pairs_per_gpu": n_per,
+            "config": {"workload": (WORKLOAD_NAME if args.config == 2 and args.pairs is None else
+                                    f"config {args.config}, {n_per} pairs per GPU") +
+                       (" in CIGAR mode" if args.cigar else ""), "pairs_per_gpu": n_per,
                        "scoring": list(SCORING), "form": "batched persistent",
                        "cache": "inputs larger than L2 (2.6 GB resident per GPU)", "parallelism": f"replicas x{ws}"},
             "alignments_per_s": pairs_all / (ms * 1e-3),

@@ -30,9 +30,11 @@
 // generic kernel (rows and directions in global memory, host-driven rounds).  Directions
 // take 4 bits per cell (E open/extend, F open/extend, H source) written one row word at
 // a time, coalesced across the warp ([row][word][thread] layout).  The traceback walks
-// the stored directions three times (the walk's end column, then the op count and
-// mismatches, then the ops themselves written back to front), so each pair's ops go
-// straight to their place in a shared arena reserved with one atomic per warp.
+// the stored directions once, streaming the rows it visits through a ring of prefetched
+// row words and recording its steps (2 bits each) in thread-local memory; replaying the
+// record counts the ops and mismatches, then writes the ops back to front straight to
+// their place in a shared arena reserved with one atomic per warp.  (The generic kernel,
+// whose walks are unbounded, walks its stored directions three times instead.)
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -59,6 +61,8 @@ struct CigarArgs {
   int64_t arena_cap;
   unsigned long long *cursor;
   int *counts;
+  uint32_t *keys, *idx;           // classification output (sort input)
+  const uint32_t *sorted;         // pairs in (class, rows descending) order
   int2 *lists;
   int64_t list_cap;
   int4 *generic;
@@ -68,46 +72,60 @@ struct CigarArgs {
 __host__ __device__ constexpr int cigar_half(int c) { return c == 0 ? 1 : c == 1 ? 3 : c == 2 ? 7 : c == 3 ? 15 : 31; }
 
 __device__ __forceinline__ int list_for(int w, int rows) {
-  if (rows > kCigarRowCap) return kCigarClasses;
+  if (rows > kCigarRowCap) return kCigarGeneric;
 #pragma unroll
   for (int c = 0; c < kCigarClasses; c++)
     if (w <= cigar_half(c)) return c;
-  return kCigarClasses;
+  return kCigarGeneric;
 }
 
 __device__ __forceinline__ int sub_score(const CigarArgs &g, int a, int b) {
   return (a == kCodeN || b == kCodeN) ? -g.amb : (a == b ? g.match : -g.mismatch);
 }
 
-// Appends (p, w) to list c (warp-aggregated counter bump per distinct list).
+// Appends (p, w) to the generic list or to register kernel c's escalation list.
 __device__ __forceinline__ void list_push(const CigarArgs &g, int c, int p, int w, int rows, int ref_len) {
-  if (c == kCigarClasses) {
-    const int at = atomicAdd(&g.counts[c], 1);
+  if (c == kCigarGeneric) {
+    const int at = atomicAdd(&g.counts[kCigarGeneric], 1);
     g.generic[at] = make_int4(p, w, rows, ref_len);
     return;
   }
-  const unsigned act = __activemask();  // the lanes on this path only
-  const unsigned peers = __match_any_sync(act, c);
-  const int leader = __ffs(peers) - 1;
-  const int lane = threadIdx.x & 31;
-  int base = 0;
-  if (lane == leader) base = atomicAdd(&g.counts[c], __popc(peers));
-  base = __shfl_sync(peers, base, leader);
-  const int rank = __popc(peers & ((1u << lane) - 1));
-  g.lists[(int64_t)c * g.list_cap + base + rank] = make_int2(p, w);
+  const int at = atomicAdd(&g.counts[kCigarEsc + c], 1);
+  g.lists[(int64_t)c * g.list_cap + at] = make_int2(p, w);
 }
 
-__global__ void k_cigar_classify(CigarArgs g, int64_t n) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
+constexpr uint32_t kKeyNone = (1u << 13) - 1;  // sorts after every (class, rows) key
+
+// order (may be null): the batched forward pass's length-sorted pair order, so pairs of
+// similar length share warps in every list.
+// Per pair: the register kernel its first band fits (key = class, then box rows
+// descending, so a warp's lanes take boxes of about the same height, longest first), or
+// the generic list.  order (may be null): the batched forward pass's pair order.
+__global__ void k_cigar_classify(CigarArgs g, int64_t n, const uint32_t *__restrict__ order) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n) return;
+  const int64_t p = order ? (int64_t)order[idx] : idx;
   g.nops[p] = 0;
   g.mism[p] = 0;
   g.op_off[p] = 0;
+  uint32_t key = kKeyNone;
   const int S = g.score[p], ab = g.a_beg[p], ae = g.a_end[p], bb = g.b_beg[p], be = g.b_end[p];
-  if (S <= 0 || ab < 0 || bb < 0 || ae - ab > 32767 || be - bb > 32767) return;
-  const int ref_len = ae - ab + 1, rows = be - bb + 1;
-  const int w = abs(ref_len - rows) + 1;
-  list_push(g, list_for(w, rows), (int)p, w, rows, ref_len);
+  if (S > 0 && ab >= 0 && bb >= 0 && ae - ab <= 32767 && be - bb <= 32767) {
+    const int ref_len = ae - ab + 1, rows = be - bb + 1;
+    const int w = abs(ref_len - rows) + 1;
+    const int c = list_for(w, rows);
+    if (c == kCigarGeneric) {
+      list_push(g, c, (int)p, w, rows, ref_len);
+    } else {
+      key = ((uint32_t)c << 10) | (uint32_t)(1023 - rows);
+      const unsigned act = __activemask();  // the lanes on this path only
+      const unsigned peers = __match_any_sync(act, c);
+      const int leader = __ffs(peers) - 1;
+      if ((int)(threadIdx.x & 31) == leader) atomicAdd(&g.counts[c], __popc(peers));
+    }
+  }
+  g.keys[idx] = key;
+  g.idx[idx] = (uint32_t)p;
 }
 
 // ---- traceback (shared by the register and the generic kernels) ----------------------
@@ -196,6 +214,23 @@ __device__ bool tb_walk(const Dir &dir, const Box &bx, int w, int mode, int j_en
   return true;
 }
 
+// Arena space for `want` ops.  warp_sync: every lane of the warp calls together and the
+// warp reserves its total with one atomic (lanes with nothing to write pass 0).
+__device__ __forceinline__ int64_t reserve_arena(const CigarArgs &g, int want, bool warp_sync) {
+  if (!warp_sync) return want > 0 ? (int64_t)atomicAdd(g.cursor, (unsigned long long)want) : 0;
+  const int lane = threadIdx.x & 31;
+  int incl = want;
+#pragma unroll
+  for (int s = 1; s < 32; s <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, s);
+    if (lane >= s) incl += v;
+  }
+  unsigned long long wb = 0;
+  if (lane == 31 && incl > 0) wb = atomicAdd(g.cursor, (unsigned long long)incl);
+  wb = __shfl_sync(0xffffffffu, wb, 31);
+  return (int64_t)wb + incl - want;
+}
+
 // Three walks: end column, count, then (after the arena reservation) the ops.  Lanes of
 // a warp reserve their arena space with one atomic; `valid` lanes with nothing to write
 // join the reservation with 0 ops.
@@ -208,29 +243,14 @@ __device__ void traceback_and_emit(const CigarArgs &g, const Dir &dir, const Box
   if (ok) ok = tb_walk(dir, bx, w, 1, j_end, &nops, &mm, nullptr, 0);
   if (valid && !ok) {
     g.nops[p] = -1;
-    atomicAdd(&g.counts[kCigarClasses + 2], 1);
+    atomicAdd(&g.counts[kCigarWalkErrors], 1);
   }
   const int want = ok ? nops : 0;
-  int64_t base;
-  if (warp_sync) {
-    const int lane = threadIdx.x & 31;
-    int incl = want;
-#pragma unroll
-    for (int s = 1; s < 32; s <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, s);
-      if (lane >= s) incl += v;
-    }
-    unsigned long long wb = 0;
-    if (lane == 31 && incl > 0) wb = atomicAdd(g.cursor, (unsigned long long)incl);
-    wb = __shfl_sync(0xffffffffu, wb, 31);
-    base = (int64_t)wb + incl - want;
-  } else {
-    base = want > 0 ? (int64_t)atomicAdd(g.cursor, (unsigned long long)want) : 0;
-  }
+  const int64_t base = reserve_arena(g, want, warp_sync);
   if (!ok) return;
   if (base + want > g.arena_cap) {  // arena full: the host grows it and runs the pass again
     g.nops[p] = -1;
-    atomicAdd(&g.counts[kCigarClasses + 1], 1);
+    atomicAdd(&g.counts[kCigarArenaFull], 1);
     return;
   }
   int t2 = 0, mm2 = 0;
@@ -242,14 +262,191 @@ __device__ void traceback_and_emit(const CigarArgs &g, const Dir &dir, const Box
 
 // ---- register-band kernels ------------------------------------------------------------
 
+// Register kernels' traceback.  The direction walk is a chain of dependent loads (each
+// step's position comes from the previous step's nibble), so it runs once: the rows it
+// visits stream through a ring of prefetched row words (P rows of NW words, P * NW = 8,
+// loaded P rows ahead of the walk), and its steps are recorded, 2 bits each, in a
+// thread-local array.  Counting and writing the ops then replay the record.
+constexpr int kPathWords = 68;  // 16 steps a word; a walk takes at most
+                                // (kCigarRowCap - 1) + (kCigarRowCap + 30 - 1) steps
+
 template <int NW>
-struct RegDir {  // directions of one thread: word (row, q) at dirs[(row * NW + q) * T + tid]
+struct RowRing {
+  static constexpr int P = 8 / NW;
+  uint32_t r[P][NW];
   const uint32_t *base;
   int64_t stride;
-  __device__ __forceinline__ uint32_t operator()(int i, int k) const {
-    return (__ldcg(base + ((int64_t)i * NW + (k >> 3)) * stride) >> ((k & 7) * 4)) & 15u;
+  __device__ __forceinline__ void load(uint32_t (&dst)[NW], int i) const {
+#pragma unroll
+    for (int q = 0; q < NW; q++) dst[q] = i >= 0 ? __ldcg(base + ((int64_t)i * NW + q) * stride) : 0u;
+  }
+  __device__ __forceinline__ void init(int top) {
+#pragma unroll
+    for (int p = 0; p < P; p++) load(r[p], top - p);
+  }
+  __device__ __forceinline__ void down(int new_top) {  // the walk moved from row new_top + 1
+#pragma unroll
+    for (int p = 0; p + 1 < P; p++)
+#pragma unroll
+      for (int q = 0; q < NW; q++) r[p][q] = r[p + 1][q];
+    load(r[P - 1], new_top - (P - 1));
+  }
+  __device__ __forceinline__ uint32_t nib(int k) const {
+    uint32_t w = r[0][0];
+#pragma unroll
+    for (int q = 1; q < NW; q++)
+      if ((k >> 3) == q) w = r[0][q];
+    return (w >> ((k & 7) * 4)) & 15u;
   }
 };
+
+// Walk 1: returns false when the walk leaves the computed band (or outgrows the record).
+template <int NW>
+__device__ bool walk_record(RowRing<NW> &ring, const Box &bx, int w, uint32_t *path, int *nsteps, int *j_end) {
+  int i = bx.rows - 1, j = bx.ref_len - 1, st = 2, n = 0;
+  ring.init(i);
+  while (i > 0) {
+    if (j < 0 || n >= kPathWords * 16) return false;
+    const int k = j - i + w;
+    if (k < 0 || k > 2 * w) return false;
+    const uint32_t nb = ring.nib(k);
+    int code;
+    if (st == 0) {
+      code = 2 + (int)(nb & 1u);
+    } else if (st == 1) {
+      code = 4 + (int)((nb >> 1) & 1u);
+    } else {
+      const uint32_t hs = nb >> 2;
+      code = hs == 0 ? 1 : hs == 1 ? 2 + (int)(nb & 1u) : hs == 2 ? 4 + (int)((nb >> 1) & 1u) : 0;
+    }
+    uint32_t op;
+    switch (code) {
+      case 1: --i; --j; st = 2; op = kOpM; break;
+      case 2: --i; st = 0; op = kOpI; break;
+      case 3: --i; st = 2; op = kOpI; break;
+      case 4: --j; st = 1; op = kOpD; break;
+      case 5: --j; st = 2; op = kOpD; break;
+      default: return false;
+    }
+    if ((n & 15) == 0) path[n >> 4] = 0u;
+    path[n >> 4] |= op << ((n & 15) * 2);
+    ++n;
+    if (op != kOpD) ring.down(i);
+  }
+  *nsteps = n;
+  *j_end = j;
+  return true;
+}
+
+// Replays the record.  mode 1: counts ops (*res) and mismatches (*mm), comparing the
+// bases of the M steps with loads issued 8 steps at a time, and keeps each M step's
+// =/X outcome in xf (1 bit a step); mode 2: writes the ops to out[0 .. nops) back to
+// front from the record and xf alone.
+__device__ void replay_path(const Box &bx, const uint32_t *path, uint32_t *xf, int nsteps, int j_end, int mode,
+                            int *res, int *mm, uint32_t *out, int nops) {
+  int t = 0, run_kind = -1, run_len = 0, mis = 0;
+  auto emit = [&](uint32_t kind, int len) {
+    if (mode == 2) out[nops - 1 - t] = ((uint32_t)len << 4) | kind;
+    ++t;
+  };
+  auto cell = [&](int kind) {
+    if (kind == run_kind) {
+      ++run_len;
+    } else {
+      if (run_len > 0) emit((uint32_t)run_kind, run_len);
+      run_kind = kind;
+      run_len = 1;
+    }
+  };
+  if (bx.tail > 0) emit(kOpS, bx.tail);
+  int ci = bx.rows - 1, cj = bx.ref_len - 1;
+  for (int s0 = 0; s0 < nsteps; s0 += 8) {
+    uint32_t xbits = 0;
+    if (mode == 1) {
+      uint32_t av[8], bv[8];
+      int i = ci, j = cj;
+#pragma unroll
+      for (int u = 0; u < 8; u++) {  // positions and independent loads of up to 8 steps
+        const int st = s0 + u;
+        const uint32_t op = st < nsteps ? (path[st >> 4] >> ((st & 15) * 2)) & 3u : kOpD;
+        av[u] = bv[u] = 0;
+        if (st < nsteps && op == kOpM) {
+          av[u] = bx.A[j - j_end];
+          bv[u] = bx.B[i];
+        }
+        i -= op != kOpD;
+        j -= op != kOpI;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u++) xbits |= (uint32_t)(av[u] != bv[u]) << u;
+      if ((s0 & 31) == 0) xf[s0 >> 5] = 0u;
+      xf[s0 >> 5] |= xbits << (s0 & 31);
+    } else {
+      xbits = (xf[s0 >> 5] >> (s0 & 31)) & 0xffu;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int st = s0 + u;
+      if (st >= nsteps) break;
+      const uint32_t op = (path[st >> 4] >> ((st & 15) * 2)) & 3u;
+      if (op == kOpM) {
+        const bool x = (xbits >> u) & 1u;
+        mis += x;
+        cell(x ? kOpX : kOpEq);
+        --ci;
+        --cj;
+      } else if (op == kOpI) {
+        ++mis;
+        cell(kOpI);
+        --ci;
+      } else {
+        ++mis;
+        cell(kOpD);
+        --cj;
+      }
+    }
+  }
+  const bool x = bx.A[0] != bx.B[0];  // the cell where the walk stopped: one more M
+  mis += x;
+  cell(x ? kOpX : kOpEq);
+  if (run_len > 0) emit((uint32_t)run_kind, run_len);
+  if (bx.bb > 0) emit(kOpS, bx.bb);
+  *res = t;
+  *mm = mis;
+}
+
+template <int NW>
+__device__ void traceback_reg(const CigarArgs &g, const uint32_t *dcol, int64_t stride, const Box &bx, int w, int p,
+                              bool valid) {
+  uint32_t path[kPathWords], xf[kPathWords / 2];
+  int nsteps = 0, j_end = 0, nops = 0, mm = 0;
+  bool ok = valid;
+  if (ok) {
+    RowRing<NW> ring;
+    ring.base = dcol;
+    ring.stride = stride;
+    ok = walk_record(ring, bx, w, path, &nsteps, &j_end);
+    if (!ok) {
+      g.nops[p] = -1;
+      atomicAdd(&g.counts[kCigarWalkErrors], 1);
+    } else {
+      replay_path(bx, path, xf, nsteps, j_end, 1, &nops, &mm, nullptr, 0);
+    }
+  }
+  const int want = ok ? nops : 0;
+  const int64_t base = reserve_arena(g, want, true);
+  if (!ok) return;
+  if (base + want > g.arena_cap) {  // arena full: the host grows it and runs the pass again
+    g.nops[p] = -1;
+    atomicAdd(&g.counts[kCigarArenaFull], 1);
+    return;
+  }
+  int t2 = 0, mm2 = 0;
+  replay_path(bx, path, xf, nsteps, j_end, 2, &t2, &mm2, g.arena + base, nops);
+  g.op_off[p] = base;
+  g.nops[p] = nops;
+  g.mism[p] = mm;
+}
 
 // One banded DP pass at half-width w <= W; returns the band's maximum.
 template <int W>
@@ -332,10 +529,14 @@ __global__ void __launch_bounds__(128) k_cigar_band(CigarArgs g) {
   constexpr int NW = (2 * W + 1 + 7) / 8;
   const int64_t T = (int64_t)gridDim.x * blockDim.x;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int count = g.counts[C];
+  // this kernel's segment of the sorted pairs, then its escalation list
+  int seg0 = 0;
+#pragma unroll
+  for (int c = 0; c < C; c++) seg0 += g.counts[c];
+  const int seg_n = g.counts[C];
+  const int count = seg_n + g.counts[kCigarEsc + C];
   const int2 *list = g.lists + (int64_t)C * g.list_cap;
   uint32_t *dcol = g.dirs + tid;
-  const RegDir<NW> dir{dcol, T};
   // warp-uniform trip count: every lane reaches the arena reservation together
   for (int64_t base = tid - (threadIdx.x & 31); base < count; base += T) {
     const int64_t e = base + (threadIdx.x & 31);
@@ -343,10 +544,16 @@ __global__ void __launch_bounds__(128) k_cigar_band(CigarArgs g) {
     int p = 0, w = 0;
     Box bx{};
     if (valid) {
-      const int2 ent = list[e];
-      p = ent.x;
-      w = ent.y;
-      bx = make_box(g, p);
+      if (e < seg_n) {
+        p = (int)g.sorted[seg0 + e];
+        bx = make_box(g, p);
+        w = abs(bx.ref_len - bx.rows) + 1;
+      } else {
+        const int2 ent = list[e - seg_n];
+        p = ent.x;
+        w = ent.y;
+        bx = make_box(g, p);
+      }
       const int S = g.score[p];
       for (;;) {
         if (w > W) {
@@ -359,7 +566,7 @@ __global__ void __launch_bounds__(128) k_cigar_band(CigarArgs g) {
       }
     }
     __syncwarp();
-    traceback_and_emit(g, dir, bx, w, p, valid, true);
+    traceback_reg<NW>(g, dcol, T, bx, w, p, valid);
   }
 }
 
@@ -443,7 +650,7 @@ __global__ void k_cigar_any(CigarArgs g, const int4 *entries, int count, int thr
     }
     if (!ok) {
       g.nops[p] = -1;
-      atomicAdd(&g.counts[kCigarClasses + 2], 1);
+      atomicAdd(&g.counts[kCigarWalkErrors], 1);
       continue;
     }
     int *Hs = reinterpret_cast<int *>(my);
@@ -499,6 +706,9 @@ CigarArgs make_args(const PairSet &ps, const ResultSet &rs, const Scoring &sc, c
   g.arena_cap = cb.arena_cap;
   g.cursor = cb.cursor;
   g.counts = cb.counts;
+  g.keys = cb.keys_in;
+  g.idx = cb.idx_in;
+  g.sorted = cb.idx_out;
   g.lists = cb.lists;
   g.list_cap = cb.list_cap;
   g.generic = cb.generic;
@@ -520,19 +730,25 @@ cudaError_t launch_band(const CigarArgs &g, int sms, size_t dirs_bytes, cudaStre
 }  // namespace
 
 cudaError_t launch_cigar(const PairSet &ps, const ResultSet &rs, const Scoring &sc, const CigarBufs &cb, int sms,
-                         cudaStream_t st, int64_t *launches) {
+                         const uint32_t *order, cudaStream_t st, int64_t *launches) {
   const CigarArgs g = make_args(ps, rs, sc, cb);
   k_cigar_reset<<<1, 32, 0, st>>>(cb.counts, cb.cursor);
   const int64_t n = ps.n;
-  if (n > 0) k_cigar_classify<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, n);
+  if (n > 0) k_cigar_classify<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g, n, order);
   cudaError_t e = cudaGetLastError();
   if (e) return e;
+  if (n > 0) {
+    size_t tb = cb.sort_temp_bytes;
+    e = cub::DeviceRadixSort::SortPairs(cb.sort_temp, tb, cb.keys_in, cb.keys_out, cb.idx_in, cb.idx_out, (int)n, 0,
+                                        13, st);
+    if (e) return e;
+  }
   if ((e = launch_band<0>(g, sms, cb.dirs_bytes, st))) return e;
   if ((e = launch_band<1>(g, sms, cb.dirs_bytes, st))) return e;
   if ((e = launch_band<2>(g, sms, cb.dirs_bytes, st))) return e;
   if ((e = launch_band<3>(g, sms, cb.dirs_bytes, st))) return e;
   if ((e = launch_band<4>(g, sms, cb.dirs_bytes, st))) return e;
-  if (launches) *launches += 2 + kCigarClasses;
+  if (launches) *launches += 2 + kCigarClasses + 4;  // + the radix sort's passes (approximate)
   return cudaSuccess;
 }
 
@@ -545,6 +761,13 @@ cudaError_t launch_cigar_generic(const PairSet &ps, const ResultSet &rs, const S
   const int blocks = (threads + block - 1) / block;
   k_cigar_any<<<blocks, block, 0, st>>>(g, entries, count, threads, static_cast<unsigned char *>(pool), slice);
   return cudaGetLastError();
+}
+
+cudaError_t cigar_sort_temp_bytes(int64_t n, size_t *bytes) {
+  *bytes = 0;
+  return cub::DeviceRadixSort::SortPairs(nullptr, *bytes, (const uint32_t *)nullptr, (uint32_t *)nullptr,
+                                         (const uint32_t *)nullptr, (uint32_t *)nullptr, (int)std::max<int64_t>(n, 1),
+                                         0, 13);
 }
 
 cudaError_t cigar_gather_temp_bytes(int64_t n, size_t *bytes) {

@@ -126,6 +126,8 @@ struct mhsw_driver {
   DBuf<int> c_counts;
   DBuf<int2> c_lists;
   DBuf<int4> c_generic, c_gsorted;
+  DBuf<uint32_t> c_keys_in, c_keys_out, c_idx_in, c_idx_out;
+  DBuf<unsigned char> c_sort_temp;
   DBuf<unsigned char> c_pool, c_temp;
   HBuf<int> h_ccounts;
   cudaEvent_t ev_c[2] = {nullptr, nullptr};
@@ -221,6 +223,11 @@ struct mhsw_driver {
     c_lists.release();
     c_generic.release();
     c_gsorted.release();
+    c_keys_in.release();
+    c_keys_out.release();
+    c_idx_in.release();
+    c_idx_out.release();
+    c_sort_temp.release();
     c_pool.release();
     c_temp.release();
     h_ccounts.release();
@@ -328,6 +335,13 @@ int ensure_cigar(mhsw_driver *d, int64_t n) {
   // 32 ops per pair on average before the arena has to grow (finish_cigar grows it)
   MHSW_CK(d->c_arena.reserve(std::max<size_t>((size_t)n * 32, 1 << 16)), "cudaMalloc CIGAR arena");
   MHSW_CK(d->h_ccounts.reserve(mhsw::kCigarCounters + 2), "cudaMallocHost");
+  MHSW_CK(d->c_keys_in.reserve((size_t)n + 1), "cudaMalloc CIGAR sort");
+  MHSW_CK(d->c_keys_out.reserve((size_t)n + 1), "cudaMalloc CIGAR sort");
+  MHSW_CK(d->c_idx_in.reserve((size_t)n + 1), "cudaMalloc CIGAR sort");
+  MHSW_CK(d->c_idx_out.reserve((size_t)n + 1), "cudaMalloc CIGAR sort");
+  size_t tb = 0;
+  MHSW_CK(mhsw::cigar_sort_temp_bytes(n, &tb), "CIGAR sort size");
+  MHSW_CK(d->c_sort_temp.reserve(tb + 256), "cudaMalloc CIGAR sort");
   return MHSW_OK;
 }
 
@@ -340,6 +354,12 @@ mhsw::CigarBufs cigar_bufs(mhsw_driver *d, int64_t n) {
   cb.arena_cap = (int64_t)d->c_arena.cap;
   cb.cursor = d->c_cursor.p;
   cb.counts = d->c_counts.p;
+  cb.keys_in = d->c_keys_in.p;
+  cb.keys_out = d->c_keys_out.p;
+  cb.idx_in = d->c_idx_in.p;
+  cb.idx_out = d->c_idx_out.p;
+  cb.sort_temp = d->c_sort_temp.p;
+  cb.sort_temp_bytes = d->c_sort_temp.cap;
   cb.lists = d->c_lists.p;
   cb.list_cap = n + 1;
   cb.generic = d->c_generic.p;
@@ -351,7 +371,8 @@ mhsw::CigarBufs cigar_bufs(mhsw_driver *d, int64_t n) {
 // Classification and the register-band kernels, then the counters' copy to the host
 // (all stream-ordered; part of a captured graph when the batch is captured).
 int enqueue_cigar(mhsw_driver *d, const mhsw::PairSet &ps) {
-  MHSW_CK(mhsw::launch_cigar(ps, result_set(d), d->sc, cigar_bufs(d, ps.n), d->sms, d->st, &d->launches),
+  MHSW_CK(mhsw::launch_cigar(ps, result_set(d), d->sc, cigar_bufs(d, ps.n), d->sms, d->fwd_order, d->st,
+                              &d->launches),
           "CIGAR launch");
   MHSW_CK(cudaMemcpyAsync(d->h_ccounts.p, d->c_counts.p, sizeof(int) * mhsw::kCigarCounters, cudaMemcpyDeviceToHost,
                           d->st),
@@ -370,7 +391,7 @@ int finish_cigar(mhsw_driver *d, const mhsw::PairSet &ps) {
   bool generic_done = false;
   for (int round = 0; round < 4; round++) {
     const int *cnt = d->h_ccounts.p;
-    if (cnt[mhsw::kCigarClasses + 1] > 0) {  // arena full: grow to what was asked for, run again
+    if (cnt[mhsw::kCigarArenaFull] > 0) {  // arena full: grow to what was asked for, run again
       unsigned long long need = 0;
       MHSW_CK(cudaMemcpy(&need, d->c_cursor.p, sizeof(need), cudaMemcpyDeviceToHost), "D2H cursor");
       MHSW_CK(d->c_arena.reserve((size_t)need + (size_t)n * 8 + 1024), "cudaMalloc CIGAR arena");
@@ -380,7 +401,7 @@ int finish_cigar(mhsw_driver *d, const mhsw::PairSet &ps) {
       generic_done = false;
       continue;
     }
-    const int ng = cnt[mhsw::kCigarClasses];
+    const int ng = cnt[mhsw::kCigarGeneric];
     if (ng > 0 && !generic_done) {
       generic_done = true;
       d->cigar_generic = ng;
@@ -418,7 +439,7 @@ int finish_cigar(mhsw_driver *d, const mhsw::PairSet &ps) {
     }
     break;
   }
-  if (d->h_ccounts.p[mhsw::kCigarClasses + 1] > 0)
+  if (d->h_ccounts.p[mhsw::kCigarArenaFull] > 0)
     return d->fail(MHSW_ERR_INTERNAL, "CIGAR arena still full after growing it");
   d->cigar_n = n;
   d->cigar_total = -1;

@@ -109,9 +109,15 @@ cudaError_t launch_pack5(const ResultSet &rs, int64_t n, int32_t *out5, cudaStre
 // ---- CIGAR pass (mhsw_cigar.cu) ----------------------------------------------------
 constexpr int kCigarClasses = 5;     // register-band traceback kernels, half-widths 1, 3, 7, 15, 31
 constexpr int kCigarRowCap = 512;    // box rows those kernels keep directions for
-// Counters: [0 .. kCigarClasses-1] class list sizes, [kCigarClasses] generic list size,
-// [+1] pairs that found the arena full, [+2] tracebacks that left the computed band.
-constexpr int kCigarCounters = kCigarClasses + 3;
+// Counters: [0 .. kCigarClasses-1] pairs each register kernel takes first (its segment of
+// the sorted pair order), then the generic list size, pairs that found the arena full,
+// tracebacks that left the computed band, and [kCigarEsc ..] each register kernel's
+// escalation list size (pairs whose band outgrew a narrower kernel).
+constexpr int kCigarGeneric = kCigarClasses;
+constexpr int kCigarArenaFull = kCigarClasses + 1;
+constexpr int kCigarWalkErrors = kCigarClasses + 2;
+constexpr int kCigarEsc = kCigarClasses + 3;
+constexpr int kCigarCounters = kCigarEsc + kCigarClasses;
 constexpr size_t kCigarDirBudget = size_t(256) << 20;  // direction scratch of the register kernels
 
 // Generic-kernel slice of one pair at half-width w: H and E rows plus 4-bit directions.
@@ -126,7 +132,10 @@ struct CigarBufs {           // device buffers of the CIGAR pass
   int64_t arena_cap;
   unsigned long long *cursor;
   int *counts;               // kCigarCounters
-  int2 *lists;               // kCigarClasses segments of list_cap (pair, half-width) entries
+  uint32_t *keys_in, *keys_out, *idx_in, *idx_out;  // n each: (class, rows) sort of the pairs
+  void *sort_temp;
+  size_t sort_temp_bytes;
+  int2 *lists;               // kCigarClasses escalation lists of list_cap (pair, half-width) entries
   int64_t list_cap;
   int4 *generic;             // generic list: (pair, half-width, rows, columns), list_cap entries
   uint32_t *dirs;            // direction scratch, dirs_bytes
@@ -134,9 +143,12 @@ struct CigarBufs {           // device buffers of the CIGAR pass
 };
 
 // Classification and the register-band kernels (no host synchronisation).  Pairs left
-// for the generic kernel are in cb.generic (count in cb.counts[kCigarClasses]).
+// for the generic kernel are in cb.generic (count in cb.counts[kCigarGeneric]).  order
+// (may be null): a pair order to classify in (the batched forward pass's sorted order).
 cudaError_t launch_cigar(const PairSet &ps, const ResultSet &rs, const Scoring &sc, const CigarBufs &cb, int sms,
-                         cudaStream_t st, int64_t *launches);
+                         const uint32_t *order, cudaStream_t st, int64_t *launches);
+// Temporary bytes of the (class, rows) sort of n pairs.
+cudaError_t cigar_sort_temp_bytes(int64_t n, size_t *bytes);
 // Generic kernel over `count` entries (device copy), `threads` threads with a slice of
 // `slice` bytes each in `pool`.
 cudaError_t launch_cigar_generic(const PairSet &ps, const ResultSet &rs, const Scoring &sc, const CigarBufs &cb,
