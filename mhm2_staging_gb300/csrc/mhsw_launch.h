@@ -107,16 +107,18 @@ cudaError_t launch_finalize(const ResultSet &rs, int64_t n, bool a_is_query, int
 cudaError_t launch_pack5(const ResultSet &rs, int64_t n, int32_t *out5, cudaStream_t st);
 
 // ---- CIGAR pass (mhsw_cigar.cu) ----------------------------------------------------
-constexpr int kCigarClasses = 5;     // register-band traceback kernels, half-widths 1, 3, 7, 15, 31
+constexpr int kCigarClasses = 6;     // register-band traceback kernels, half-widths 1, 2, 4, 8, 16, 31
 constexpr int kCigarRowCap = 512;    // box rows those kernels keep directions for
-// Counters: [0 .. kCigarClasses-1] pairs each register kernel takes first (its segment of
-// the sorted pair order), then the generic list size, pairs that found the arena full,
-// tracebacks that left the computed band, and [kCigarEsc ..] each register kernel's
-// escalation list size (pairs whose band outgrew a narrower kernel).
-constexpr int kCigarGeneric = kCigarClasses;
-constexpr int kCigarArenaFull = kCigarClasses + 1;
-constexpr int kCigarWalkErrors = kCigarClasses + 2;
-constexpr int kCigarEsc = kCigarClasses + 3;
+// Counters: [0] diagonal boxes (their CIGAR needs no DP; the first segment of the sorted
+// pair order), [1 .. kCigarClasses] the pairs each register kernel takes first (its
+// segment), then the generic list size, pairs that found the arena full, tracebacks that
+// left the computed band, and [kCigarEsc ..] each register kernel's escalation list size
+// (pairs whose band outgrew a narrower kernel).
+constexpr int kCigarSegments = kCigarClasses + 1;
+constexpr int kCigarGeneric = kCigarSegments;
+constexpr int kCigarArenaFull = kCigarSegments + 1;
+constexpr int kCigarWalkErrors = kCigarSegments + 2;
+constexpr int kCigarEsc = kCigarSegments + 3;
 constexpr int kCigarCounters = kCigarEsc + kCigarClasses;
 constexpr size_t kCigarDirBudget = size_t(256) << 20;  // direction scratch of the register kernels
 
