@@ -142,6 +142,34 @@ class GPUDriver {
     return r.score2_32;
   }
 
+  // CIGAR mode: the run_kernel_backwards / kernel_block round also computes what SSW's
+  // Aligner::Align returns with report_cigar (klign's post-assembly SAM output,
+  // src/klign.cpp:257-271, which its GPU path cannot produce, src/klign.cpp:589-600).
+  void set_cigar(bool on) { detail::check(mhsw_driver_set_cigar(drv_, on ? 1 : 0), drv_, "set_cigar"); }
+  // After kernel_block in CIGAR mode: SSW's cigar_string and mismatches per pair ("" and 0
+  // for a score of 0).
+  void get_cigars(std::vector<std::string> &cigars, std::vector<int32_t> &mismatches) {
+    int64_t total = 0;
+    detail::check(mhsw_last_cigar(drv_, nullptr, nullptr, nullptr, nullptr, 0, &total, 1), drv_, "last_cigar");
+    const size_t n = rl_.size();
+    std::vector<int32_t> nops(n);
+    std::vector<int64_t> off(n + 1);
+    std::vector<uint32_t> ops((size_t)total + 1);
+    mismatches.resize(n);
+    detail::check(mhsw_last_cigar(drv_, nops.data(), mismatches.data(), off.data(), ops.data(), (int64_t)ops.size(),
+                                  &total, 1),
+                  drv_, "last_cigar");
+    cigars.assign(n, std::string());
+    std::vector<char> buf;
+    for (size_t i = 0; i < n; i++) {
+      if (nops[i] <= 0) continue;
+      buf.resize((size_t)nops[i] * 12 + 1);
+      const int64_t len = mhsw_cigar_format(ops.data() + off[i], nops[i], buf.data(), (int64_t)buf.size());
+      if (len < 0) throw std::runtime_error("adept_sw::GPUDriver::get_cigars: format failed");
+      cigars[i].assign(buf.data(), (size_t)len);
+    }
+  }
+
   void run_kernel_forwards(std::vector<std::string> &reads, std::vector<std::string> &contigs, unsigned maxReadSize,
                            unsigned maxContigSize) {
     marshal(reads, contigs);

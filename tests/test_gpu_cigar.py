@@ -220,3 +220,48 @@ def test_cigar_off_again(built):
     d.align_pairs(pairs)
     with pytest.raises(RuntimeError, match="status 3"):
         d.last_cigar(pairs.n)
+
+
+def test_cigar_through_cpp_dropin_header(built, tmp_path):
+    """A klign-style C++ caller of include/adept-sw/driver.hpp: forwards, backwards,
+    kernel_block, then SSW's cigar_string and mismatches per pair."""
+    import shutil
+    import subprocess
+
+    from mhm2_staging_gb300 import build as mbuild
+
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    root = Path(__file__).resolve().parent.parent
+    src = tmp_path / "cigar_driver.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include <string>
+#include <vector>
+#include "adept-sw/driver.hpp"
+int main() {
+  adept_sw::GPUDriver drv;
+  drv.init(0, 1, 2, -4, -4, -2, 300);  // klign's scoring when it asks for CIGARs
+  drv.set_ambiguity(-1);
+  drv.set_cigar(true);
+  std::vector<std::string> reads = {"AAAATTTTCCCCGGGG", "AAAATTTTCCCCGGGG", "ACGT"};
+  std::vector<std::string> ctgs = {"GCTAAAATTTTCCCCGGGGACT", "AAAATTTTACCCCGGGG", "NNNN"};
+  drv.run_kernel_forwards(reads, ctgs, 16, 22);
+  drv.kernel_block();
+  drv.run_kernel_backwards(reads, ctgs, 16, 22);
+  drv.kernel_block();
+  std::vector<std::string> cig;
+  std::vector<int32_t> mm;
+  drv.get_cigars(cig, mm);
+  for (size_t i = 0; i < cig.size(); i++) std::printf("%s %d\n", cig[i].c_str(), mm[i]);
+  return 0;
+}
+''')
+    exe = tmp_path / "cigar_driver"
+    lib = mbuild.lib_path()
+    subprocess.run(["g++", "-std=c++14", "-O1", "-I", str(root / "include"), str(src), "-o", str(exe), str(lib),
+                    f"-Wl,-rpath,{lib.parent}"], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    # test/ssw-test.cpp:213-231 expects 3S16=3S-style clips and 8=1I8=; all-N scores 0
+    assert r.stdout.split("\n")[:3] == ["3S16=3S 0", "8=1I8= 1", " 0"], r.stdout
