@@ -278,7 +278,38 @@ def run_paths(drv, dev, torch, stream) -> dict:
     drv.set_int16_ceiling(default_ceiling)
     drv.set_score2(False)
     drv.set_cigar(False)
+    out["klign_caller_200k_candidates"] = _klign_caller_path(drv)
     return out
+
+
+def _klign_caller_path(drv, n: int = 200_000) -> dict:
+    """klign's caller side on the device (mhsw_klign_align): seed-hit candidates from host
+    arrays to klign's Aln fields in host arrays, against 64 MB of resident contigs; 1 warm-up
+    call, then 3 timed (wall clock: the call is synchronous).  Beside it the CPU
+    restatement (oracle/klign_caller.py with the C SW oracle) on the first 20,000."""
+    from mhm2_staging_gb300 import serving as S
+    from mhm2_staging_gb300.klign import ResidentContigs, generate_candidates, klign_align
+    from oracle import klign_caller
+
+    ct = S.generate_contigs(64 << 20, seed=3)
+    cand = generate_candidates(ct, n, seed=21)
+    rc = ResidentContigs(ct)
+    r = klign_align(drv, rc, cand)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        r = klign_align(drv, rc, cand)
+    dt = (time.perf_counter() - t0) / 3
+    rc.close()
+    sub = cand.slice(0, 20_000)
+    t0 = time.perf_counter()
+    klign_caller.klign_align(ct.seq, ct.off, ct.len, sub.read_seq, sub.read_off, sub.read_len, sub.cid,
+                             sub.pos_in_ctg, sub.pos_in_read, sub.strand, sub.kmer_len, SCORING, False,
+                             os.cpu_count() or 1)
+    cdt = time.perf_counter() - t0
+    return {"candidates_per_s": n / dt, "ms_per_call": dt * 1e3, "candidates": n, "aligned": r["n_aligned"],
+            "perfect_fraction": float(r["perfect"].mean()),
+            "cpu_port": {"candidates_per_s": sub.n / cdt, "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": f"first {sub.n} candidates ({cdt:.1f} s)"}}
 
 
 def _cigar_cpu_port(pairs, n: int = 20_000) -> dict:

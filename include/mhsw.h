@@ -292,6 +292,64 @@ int mhsw_server_test(mhsw_server *s, uint64_t ticket, int *done);
 int mhsw_server_wait(mhsw_server *s, uint64_t ticket, double *times3);
 int mhsw_server_stats_get(mhsw_server *s, mhsw_server_stats *out);
 
+/* ---- klign's caller side on the device ---------------------------------------- */
+/* What klign does around each aligner call, for a batch of seed-hit candidates against
+ * contigs resident on the device (klign keeps them in a DHT and caches fetched windows,
+ * src/klign.cpp:670-739):
+ *   orientation  '-' when the contig's seed k-mer and the read's differ in strand; the
+ *                read is then reverse-complemented (utils.cpp revcomp: ACGTN, IUPAC codes
+ *                to N, any other byte is an error) and the seed position mirrored
+ *                (pos_in_read = rlen - (kmer_len + pos_in_read), :684-689);
+ *   window       the read's footprint on the seed diagonal, clipped to the contig:
+ *                left = min(pos_in_read, pos_in_ctg), right = min(rlen - kmer_len -
+ *                pos_in_read, clen - pos_in_ctg - kmer_len), cstart = pos_in_ctg - left,
+ *                rstart = pos_in_read - left, overlap = left + kmer_len + right (:690-701);
+ *   perfect      window bytes equal to the read's overlap (raw byte compare, :220): no
+ *                alignment; score1 = overlap * match, rstop = rstart + overlap, cstop =
+ *                cstart + overlap (:220-230);
+ *   otherwise    the whole oriented read against the window (SSW ref = read, query =
+ *                window, :239-241 and :257), mapped as klign maps either aligner's result
+ *                (:260-263, :372-376): rstart = read begin, rstop = read end + 1, cstart =
+ *                cstart + window begin, cstop = cstart + window end + 1;
+ *   then         '-' switches the read coordinates (start = rlen - stop, stop = rlen -
+ *                start, utils.cpp switch_orient) and identity = 100 * score1 / match /
+ *                rlen (integer arithmetic, :226, :266).
+ * score2 is SSW's second-best score when the driver is in score2 mode (klign's CPU path,
+ * :267), else 0 (its GPU path, :377-378); 0 for perfect matches. */
+typedef struct mhsw_contigs mhsw_contigs;
+
+/* Uploads contigs (host pointers: bytes, offsets, lengths) to the device and translates
+ * them once; raw bytes stay for the perfect-match compare. */
+int mhsw_contigs_create(int device, const char *seq, const int64_t *off, const int32_t *len, int64_t count,
+                        mhsw_contigs **out);
+void mhsw_contigs_destroy(mhsw_contigs *c);
+
+typedef struct {   /* host pointers */
+  const char *read_seq;       /* reads as found (before orientation), concatenated */
+  const int64_t *read_off;
+  const int32_t *read_len;
+  const int32_t *contig_id;   /* contig of the seed hit */
+  const int32_t *pos_in_ctg;  /* CtgLoc::pos_in_ctg: the seed k-mer's start in the contig */
+  const int32_t *pos_in_read; /* the seed k-mer's start in the read as found */
+  const uint8_t *strand;      /* bit 0: the read's k-mer was reverse-complemented; bit 1: the contig's (CtgLoc::is_rc) */
+  int64_t n;
+  int32_t kmer_len;
+} mhsw_candidates;
+
+typedef struct {   /* host pointers, n each: klign's Aln fields */
+  int32_t *rstart, *rstop, *cstart, *cstop;
+  int32_t *score1, *score2, *identity;
+  char *orient;               /* '+' or '-' */
+  uint8_t *perfect;           /* 1: taken by the perfect-match shortcut (no alignment) */
+} mhsw_alns;
+
+/* Runs the whole caller side plus the alignments for a candidate batch with the driver's
+ * scoring, form and score2 mode; synchronous.  Fails with MHSW_ERR_ARG (nothing written)
+ * when a candidate's seed lies outside its read or contig or its read has a byte revcomp
+ * rejects; *n_aligned (may be NULL) receives how many candidates needed an alignment. */
+int mhsw_klign_align(mhsw_driver *drv, const mhsw_contigs *contigs, const mhsw_candidates *cand, mhsw_alns *out,
+                     int64_t *n_aligned);
+
 /* ---- allocation-free forward pass (no counterpart in the reference) ---------- */
 /* Forward pass only -- score, a_end, b_end per pair, the same values as columns 0, 2
  * and 4 of mhsw_align_pairs -- for callers that must not have the library allocate

@@ -1441,6 +1441,8 @@ int align_resident(mhsw_driver *d, const PairSet &in, int64_t a_bytes, int max_a
   d->launches += 1;
   PairSet ps = in;
   ps.a_code = d->a_code.p;
+  rc = attach_score2(d, &ps, n, a_bytes);
+  if (rc) return rc;
   rc = forward_any(d, ps, max_a, max_b, form);
   if (rc) return rc;
   rc = run_reverse(d, ps, max_a, max_b, d->fwd_order);
@@ -1452,5 +1454,10 @@ int align_resident(mhsw_driver *d, const PairSet &in, int64_t a_bytes, int max_a
 
 void *driver_stream(mhsw_driver *d) { return d ? static_cast<void *>(d->st) : nullptr; }
 int driver_device(mhsw_driver *d) { return d ? d->device : -1; }
+int driver_form(mhsw_driver *d) { return d ? d->form : MHSW_FORM_PLAIN; }
+int driver_match(mhsw_driver *d) { return d ? d->sc.match : 1; }
+const int32_t *driver_score2(mhsw_driver *d, int64_t n) {
+  return (d && d->score2 && d->score2_n == n && n > 0) ? d->r_score2.p : nullptr;
+}
 
 }  // namespace mhsw

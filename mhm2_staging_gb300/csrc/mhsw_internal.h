@@ -20,5 +20,11 @@ int align_resident(mhsw_driver *d, const PairSet &ps, int64_t a_bytes, int max_a
 // The handle's stream (cudaStream_t) and device.
 void *driver_stream(mhsw_driver *d);
 int driver_device(mhsw_driver *d);
+// The handle's form for batch calls (MHSW_FORM_*) and match score.
+int driver_form(mhsw_driver *d);
+int driver_match(mhsw_driver *d);
+// Second-best scores (device, n entries) of the last align_resident call when the handle
+// is in score2 mode, else null.
+const int32_t *driver_score2(mhsw_driver *d, int64_t n);
 
 }  // namespace mhsw

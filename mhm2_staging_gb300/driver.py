@@ -134,6 +134,16 @@ class ServerStats(C.Structure):
 
 
 # Every symbol include/mhsw.h declares, with its ctypes signature.
+class CandidatesT(C.Structure):
+    _fields_ = [("read_seq", _P), ("read_off", _P), ("read_len", _P), ("contig_id", _P), ("pos_in_ctg", _P),
+                ("pos_in_read", _P), ("strand", _P), ("n", C.c_int64), ("kmer_len", C.c_int32)]
+
+
+class AlnsT(C.Structure):
+    _fields_ = [("rstart", _P), ("rstop", _P), ("cstart", _P), ("cstop", _P), ("score1", _P), ("score2", _P),
+                ("identity", _P), ("orient", _P), ("perfect", _P)]
+
+
 SIGNATURES: dict[str, tuple] = {
     "mhsw_get_num_node_gpus": (C.c_int, [C.POINTER(C.c_int)]),
     "mhsw_get_tot_gpu_mem": (C.c_int, [C.POINTER(C.c_size_t)]),
@@ -177,6 +187,9 @@ SIGNATURES: dict[str, tuple] = {
         C.c_int,
         [C.POINTER(PairsT), C.c_short, C.c_short, C.c_short, C.c_short, C.c_short, _P, _P, C.c_char_p, C.c_size_t],
     ),
+    "mhsw_contigs_create": (C.c_int, [C.c_int, _P, _P, _P, C.c_int64, C.POINTER(_P)]),
+    "mhsw_contigs_destroy": (None, [_P]),
+    "mhsw_klign_align": (C.c_int, [_P, _P, C.POINTER(CandidatesT), C.POINTER(AlnsT), C.POINTER(C.c_int64)]),
     "mhsw_probe_dpx_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "mhsw_probe_op_rate": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
 }

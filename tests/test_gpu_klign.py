@@ -1,0 +1,89 @@
+"""klign's caller side on the GPU (mhsw_klign_align): orientation, windows, the
+perfect-match shortcut, the alignments and klign's Aln mapping, bit-exact against the
+CPU restatement (oracle/klign_caller.py) on seeded candidates."""
+import numpy as np
+import pytest
+
+from mhm2_staging_gb300 import FORM_BATCHED, FORM_PLAIN, GPUDriver
+from mhm2_staging_gb300 import serving as S
+from mhm2_staging_gb300.klign import Candidates, ResidentContigs, generate_candidates, klign_align
+from oracle import klign_caller
+
+pytestmark = pytest.mark.gpu
+FIELDS = ("rstart", "rstop", "cstart", "cstop", "score1", "score2", "identity", "orient", "perfect")
+
+
+@pytest.fixture(scope="module")
+def contigs(built):
+    return S.generate_contigs(32 << 20, seed=3)
+
+
+@pytest.fixture(scope="module")
+def resident(contigs):
+    rc = ResidentContigs(contigs)
+    yield rc
+    rc.close()
+
+
+def _driver(sc=(1, 3, 5, 2, 2), form=FORM_BATCHED, score2=False):
+    m, x, go, ge, amb = sc
+    d = GPUDriver()
+    d.init(0, 1, m, -x, -go, -ge, 0)
+    d.set_ambiguity(-amb)
+    d.set_form(form)
+    d.set_score2(score2)
+    return d
+
+
+def _want(ct, cand, sc, score2):
+    return klign_caller.klign_align(ct.seq, ct.off, ct.len, cand.read_seq, cand.read_off, cand.read_len, cand.cid,
+                                    cand.pos_in_ctg, cand.pos_in_read, cand.strand, cand.kmer_len, sc, score2)
+
+
+def _diff(got, want):
+    for k in FIELDS:
+        bad = np.nonzero(got[k] != want[k])[0]
+        if len(bad):
+            i = int(bad[0])
+            return f"{k}: {len(bad)} differ; first {i}: gpu {got[k][i]} oracle {want[k][i]}"
+    return "" if got["n_aligned"] == want["n_aligned"] else f"n_aligned {got['n_aligned']} vs {want['n_aligned']}"
+
+
+@pytest.mark.parametrize("form", [FORM_PLAIN, FORM_BATCHED])
+@pytest.mark.parametrize("sc,score2", [((1, 3, 5, 2, 2), False), ((2, 4, 4, 2, 1), True)])
+def test_klign_caller_matches_restatement(contigs, resident, form, sc, score2):
+    cand = generate_candidates(contigs, 30000, seed=21)
+    got = klign_align(_driver(sc, form, score2), resident, cand)
+    want = _want(contigs, cand, sc, score2)
+    assert not _diff(got, want)
+    assert 0.3 < got["perfect"].mean() < 0.6 and got["n_aligned"] > 10000
+
+
+def test_klign_caller_k21_and_all_reverse(contigs, resident):
+    cand = generate_candidates(contigs, 5000, seed=2, kmer_len=21, minus_frac=1.0, exact_frac=0.1)
+    got = klign_align(_driver(), resident, cand)
+    assert not _diff(got, _want(contigs, cand, (1, 3, 5, 2, 2), False))
+    assert (got["orient"] == ord("-")).all()
+
+
+def test_klign_caller_rejects_bad_candidates(contigs, resident):
+    d = _driver()
+    cand = generate_candidates(contigs, 10, seed=5)
+    bad = cand.slice(0, 10)
+    bad.pos_in_read[3] = bad.read_len[3] - bad.kmer_len + 1  # seed past the read's end
+    with pytest.raises(RuntimeError, match="status 2"):
+        klign_align(d, resident, bad)
+    bad = cand.slice(0, 10)
+    bad.pos_in_ctg[2] = contigs.len[bad.cid[2]]  # seed past the contig's end
+    with pytest.raises(RuntimeError, match="status 2"):
+        klign_align(d, resident, bad)
+    seq = cand.read_seq.copy()
+    seq[cand.read_off[4] + 1] = ord("a")  # revcomp rejects lower case
+    bad = Candidates(seq, cand.read_off, cand.read_len, cand.cid, cand.pos_in_ctg, cand.pos_in_read, cand.strand,
+                     cand.kmer_len)
+    with pytest.raises(RuntimeError, match="status 2"):
+        klign_align(d, resident, bad)
+    # the driver is still usable afterwards, and an empty batch is fine
+    got = klign_align(d, resident, cand)
+    assert not _diff(got, _want(contigs, cand, (1, 3, 5, 2, 2), False))
+    assert klign_align(d, resident, cand.slice(0, 0))["n_aligned"] == 0
