@@ -279,7 +279,64 @@ def run_paths(drv, dev, torch, stream) -> dict:
     drv.set_score2(False)
     drv.set_cigar(False)
     out["klign_caller_200k_candidates"] = _klign_caller_path(drv)
+    out["protein_100k_pairs_100_500aa"] = _protein_path()
     return out
+
+
+def _protein_pairs(n: int, seed: int = 8):
+    """Seeded protein pairs: A of U[100, 500] residues; B = A with 10% substitutions and 2%
+    deletions between random flanks (one pair in three unrelated)."""
+    from mhm2_staging_gb300 import Pairs
+    from oracle import oracle
+
+    letters = np.frombuffer(oracle.PROTEIN_LETTERS.encode(), dtype=np.uint8)
+    rng = np.random.default_rng(seed)
+    a, b = [], []
+    for k in range(n):
+        x = letters[rng.integers(0, 20, int(rng.integers(100, 501)))]
+        if k % 3 == 0:
+            y = letters[rng.integers(0, 20, int(rng.integers(100, 501)))]
+        else:
+            y = x.copy()
+            sub = rng.random(y.shape[0]) < 0.1
+            y[sub] = letters[rng.integers(0, 24, int(sub.sum()))]
+            y = y[rng.random(y.shape[0]) > 0.02]
+            y = np.concatenate([letters[rng.integers(0, 20, int(rng.integers(0, 40)))], y,
+                                letters[rng.integers(0, 20, int(rng.integers(0, 40)))]])
+        a.append(x.tobytes())
+        b.append(y.tobytes())
+    return Pairs.from_lists(a, b)
+
+
+def _protein_path(n: int = 100_000) -> dict:
+    """Protein alignment (mhsw_align_protein, host arrays in and out) with a seeded 24 x 24
+    matrix (diagonal 4..11, elsewhere -4..3), gaps 11/1; 1 warm-up call, 3 timed (wall
+    clock, synchronous call).  GCUPS count the forward cells.  Beside it the oracle port
+    on the first 2,000 pairs."""
+    from mhm2_staging_gb300 import GPUDriver
+    from oracle import oracle
+
+    pairs = _protein_pairs(n)
+    rng = np.random.default_rng(2024)
+    m = rng.integers(-4, 4, (24, 24))
+    m = (np.triu(m) + np.triu(m, 1).T).astype(np.int16)
+    np.fill_diagonal(m, rng.integers(4, 12, 24))
+    enc = oracle.protein_encoding()
+    d = GPUDriver()
+    d.init(0, 1, 1, -1, -11, -1, 0)
+    d.align_protein(pairs, m, enc)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        d.align_protein(pairs, m, enc)
+    dt = (time.perf_counter() - t0) / 3
+    cells = float(pairs.cells())
+    sub = pairs.slice(0, 2000)
+    t0 = time.perf_counter()
+    oracle.protein_batch(sub, m, enc, 11, 1, os.cpu_count() or 1)
+    cdt = time.perf_counter() - t0
+    return {"gcups": cells / dt / 1e9, "ms_per_call": dt * 1e3, "pairs": n, "cells": cells,
+            "cpu_port": {"gcups": float(sub.cells()) / cdt / 1e9, "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": f"first {sub.n} pairs ({cdt:.1f} s)"}}
 
 
 def _klign_caller_path(drv, n: int = 200_000) -> dict:

@@ -350,6 +350,18 @@ typedef struct {   /* host pointers, n each: klign's Aln fields */
 int mhsw_klign_align(mhsw_driver *drv, const mhsw_contigs *contigs, const mhsw_candidates *cand, mhsw_alns *out,
                      int64_t *n_aligned);
 
+/* ---- protein alignment ---------------------------------------------------------- */
+/* The reference declares protein kernels (src/adept-sw/kernel.cpp:510-899,
+ * sequence_aa_kernel / sequence_aa_reverse) that take a 24 x 24 scoring matrix and a
+ * 91-entry ASCII encoding (byte -> matrix index) from their caller; nothing in MHM2
+ * launches them.  mhsw_align_protein computes their outputs -- score, a_begin, a_end,
+ * b_begin, b_end per pair, laid out as mhsw_align_pairs -- with SSW's result rules (the
+ * DNA path's) and the handle's gap penalties: matrix[a * 24 + b] scores A's code a against
+ * B's code b.  Bytes >= 91 or encodings outside [0, 24) fail with MHSW_ERR_ARG.  Pairs
+ * and out5 are host or device pointers as host_io says; synchronous. */
+int mhsw_align_protein(mhsw_driver *drv, const mhsw_pairs *pairs, const int16_t *scoring_matrix,
+                       const int16_t *encoding, int32_t *out5, int host_io);
+
 /* ---- allocation-free forward pass (no counterpart in the reference) ---------- */
 /* Forward pass only -- score, a_end, b_end per pair, the same values as columns 0, 2
  * and 4 of mhsw_align_pairs -- for callers that must not have the library allocate

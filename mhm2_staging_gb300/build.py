@@ -23,7 +23,7 @@ BUILD = PKG / "_build"
 INCLUDE = ROOT / "include"
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_UNITS = ["mhsw_kernels.cu", "mhsw_batch.cu", "mhsw_driver.cu", "mhsw_probe.cu", "mhsw_noalloc.cu", "mhsw_cigar.cu", "mhsw_klign.cu",
+CUDA_UNITS = ["mhsw_kernels.cu", "mhsw_batch.cu", "mhsw_driver.cu", "mhsw_probe.cu", "mhsw_noalloc.cu", "mhsw_cigar.cu", "mhsw_klign.cu", "mhsw_protein.cu",
               "mhsw_server.cu"]
 
 

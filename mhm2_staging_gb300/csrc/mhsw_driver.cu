@@ -1456,6 +1456,10 @@ void *driver_stream(mhsw_driver *d) { return d ? static_cast<void *>(d->st) : nu
 int driver_device(mhsw_driver *d) { return d ? d->device : -1; }
 int driver_form(mhsw_driver *d) { return d ? d->form : MHSW_FORM_PLAIN; }
 int driver_match(mhsw_driver *d) { return d ? d->sc.match : 1; }
+void driver_gaps(mhsw_driver *d, int *gap_open, int *gap_extend) {
+  *gap_open = d ? d->sc.gap_open : 0;
+  *gap_extend = d ? d->sc.gap_extend : 0;
+}
 const int32_t *driver_score2(mhsw_driver *d, int64_t n) {
   return (d && d->score2 && d->score2_n == n && n > 0) ? d->r_score2.p : nullptr;
 }

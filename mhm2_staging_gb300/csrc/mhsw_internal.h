@@ -23,6 +23,8 @@ int driver_device(mhsw_driver *d);
 // The handle's form for batch calls (MHSW_FORM_*) and match score.
 int driver_form(mhsw_driver *d);
 int driver_match(mhsw_driver *d);
+// The handle's gap penalties as positive magnitudes.
+void driver_gaps(mhsw_driver *d, int *gap_open, int *gap_extend);
 // Second-best scores (device, n entries) of the last align_resident call when the handle
 // is in score2 mode, else null.
 const int32_t *driver_score2(mhsw_driver *d, int64_t n);

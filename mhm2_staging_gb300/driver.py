@@ -187,6 +187,7 @@ SIGNATURES: dict[str, tuple] = {
         C.c_int,
         [C.POINTER(PairsT), C.c_short, C.c_short, C.c_short, C.c_short, C.c_short, _P, _P, C.c_char_p, C.c_size_t],
     ),
+    "mhsw_align_protein": (C.c_int, [_P, C.POINTER(PairsT), _P, _P, _P, C.c_int]),
     "mhsw_contigs_create": (C.c_int, [C.c_int, _P, _P, _P, C.c_int64, C.POINTER(_P)]),
     "mhsw_contigs_destroy": (None, [_P]),
     "mhsw_klign_align": (C.c_int, [_P, _P, C.POINTER(CandidatesT), C.POINTER(AlnsT), C.POINTER(C.c_int64)]),
@@ -488,6 +489,20 @@ class GPUDriver:
         results go to the device buffer out_dev_ptr (n x 5 int32)."""
         pt = dev.c_struct()
         self._ck(self._lib.mhsw_align_pairs(self._h, C.byref(pt), _P(out_dev_ptr), 0, form), "align_pairs (device)")
+
+    def align_protein(self, pairs: "Pairs", matrix: np.ndarray, encoding: np.ndarray) -> np.ndarray:
+        """Protein pairs (A = SSW ref, B = SSW query): n x 5 int32 (score, a_begin, a_end,
+        b_begin, b_end) with a 24 x 24 scoring matrix and a 91-entry byte encoding."""
+        n = pairs.n
+        out = np.zeros((n, 5), dtype=np.int32)
+        mat = np.ascontiguousarray(matrix, dtype=np.int16).reshape(-1)
+        enc = np.ascontiguousarray(encoding, dtype=np.int16)
+        if mat.shape[0] != 24 * 24 or enc.shape[0] != 91:
+            raise RuntimeError("align_protein: a 24 x 24 matrix and a 91-entry encoding")
+        pt = pairs.c_struct()
+        self._ck(self._lib.mhsw_align_protein(self._h, C.byref(pt), mat.ctypes.data, enc.ctypes.data,
+                                              out.ctypes.data if n else None, 1), "align_protein")
+        return out
 
     def last_timing(self) -> dict:
         t = Timing()

@@ -61,6 +61,9 @@ def oracle_lib() -> C.CDLL:
         _bind(lib, "sw_oracle_align_batch")
         _bind(lib, "sw_oracle_align_batch7")
         _bind_cigar(lib, "sw_oracle_cigar_batch")
+        lib.sw_oracle_protein_batch.restype = C.c_int
+        lib.sw_oracle_protein_batch.argtypes = [C.c_char_p, _P, _P, C.c_char_p, _P, _P, C.c_int64, _P, _P, C.c_int,
+                                                C.c_int, C.c_int, _P]
         lib.sw_oracle_align_codes.restype = C.c_int64
         lib.sw_oracle_align_codes.argtypes = [_P, C.c_int, _P, C.c_int, _P, C.c_int, C.c_int, _P]
         _ORACLE = lib
@@ -80,6 +83,9 @@ def ref_lib() -> C.CDLL:
         _bind(lib, "ssw_ref_align_batch")
         _bind(lib, "ssw_ref_align_batch7")
         _bind_cigar(lib, "ssw_ref_cigar_batch")
+        lib.ssw_ref_protein_batch.restype = C.c_int
+        lib.ssw_ref_protein_batch.argtypes = [C.c_char_p, _P, _P, C.c_char_p, _P, _P, C.c_int64, _P, _P, C.c_int,
+                                              C.c_int, _P]
         lib.ssw_ref_align.restype = C.c_int
         lib.ssw_ref_align.argtypes = [C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_int, C.c_int, _P]
@@ -144,6 +150,51 @@ def cigar_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, ops_
 def ref_cigar_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, ops_cap: int = 256):
     """The reference SSW with report_cigar, same layout as cigar_batch."""
     return _run_cigar(ref_lib(), "ssw_ref_cigar_batch", pairs, scoring, threads or (os.cpu_count() or 1), ops_cap)
+
+
+PROTEIN_LETTERS = "ARNDCQEGHILKMFPSTWYVBZX*"
+
+
+def protein_encoding() -> np.ndarray:
+    """A 91-entry ASCII encoding (the form the reference's protein kernels take): the 24
+    letters above to 0..23, every other byte to 22 ('X')."""
+    enc = np.full(91, PROTEIN_LETTERS.index("X"), dtype=np.int16)
+    for k, ch in enumerate(PROTEIN_LETTERS):
+        enc[ord(ch)] = k
+    return enc
+
+
+def protein_batch(pairs, mat24: np.ndarray, enc91: np.ndarray, gap_open: int, gap_extend: int,
+                  threads: int | None = None) -> np.ndarray:
+    """Oracle protein alignments n x 5 (bytes must be below 91)."""
+    n = pairs.n
+    out = np.zeros((n, 5), dtype=np.int32)
+    if n == 0:
+        return out
+    mat = np.ascontiguousarray(mat24, dtype=np.int16)
+    enc = np.ascontiguousarray(enc91, dtype=np.int16)
+    oracle_lib().sw_oracle_protein_batch(pairs.a_seq.ctypes.data_as(C.c_char_p), pairs.a_off.ctypes.data,
+                                         pairs.a_len.ctypes.data, pairs.b_seq.ctypes.data_as(C.c_char_p),
+                                         pairs.b_off.ctypes.data, pairs.b_len.ctypes.data, n, mat.ctypes.data,
+                                         enc.ctypes.data, gap_open, gap_extend, threads or (os.cpu_count() or 1),
+                                         out.ctypes.data)
+    return out
+
+
+def ref_protein_batch(pairs, mat24: np.ndarray, enc91: np.ndarray, gap_open: int, gap_extend: int) -> np.ndarray:
+    """The reference SSW with the same matrix and encoding (scores must fit int8)."""
+    n = pairs.n
+    out = np.zeros((n, 5), dtype=np.int32)
+    if n == 0:
+        return out
+    mat = np.ascontiguousarray(mat24, dtype=np.int8)
+    trans = np.zeros(128, dtype=np.int8)
+    trans[:91] = enc91
+    ref_lib().ssw_ref_protein_batch(pairs.a_seq.ctypes.data_as(C.c_char_p), pairs.a_off.ctypes.data,
+                                    pairs.a_len.ctypes.data, pairs.b_seq.ctypes.data_as(C.c_char_p),
+                                    pairs.b_off.ctypes.data, pairs.b_len.ctypes.data, n, mat.ctypes.data,
+                                    trans.ctypes.data, gap_open, gap_extend, out.ctypes.data)
+    return out
 
 
 CIGAR_OPS = "MIDNSHP=X"

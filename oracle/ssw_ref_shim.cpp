@@ -224,4 +224,30 @@ int ssw_ref_cigar_batch(const char *a_seqs, const int64_t *a_off, const int32_t 
   return 0;
 }
 
+// Protein: Aligner(score_matrix, 24, translation, 128) with SetGapPenalty, the SSW API
+// for other alphabets (ssw.hpp: "If you target for other character aligners ... pass the
+// corresponding matrix in").  out[5p..5p+4] = score, a_begin, a_end, b_begin, b_end.
+int ssw_ref_protein_batch(const char *a_seqs, const int64_t *a_off, const int32_t *a_len, const char *b_seqs,
+                          const int64_t *b_off, const int32_t *b_len, int64_t n, const int8_t *mat24,
+                          const int8_t *trans128, int gap_open, int gap_extend, int32_t *out) {
+  Aligner aligner(mat24, 24, trans128, 128);
+  aligner.SetGapPenalty((uint8_t)gap_open, (uint8_t)gap_extend);
+  Filter filter(true, false, 0, 32767);
+  Alignment aln;
+  std::string q;
+  for (int64_t p = 0; p < n; p++) {
+    q.assign(b_seqs + b_off[p], (size_t)b_len[p]);
+    const int rl = a_len[p];
+    aln.Clear();
+    aligner.Align(q.c_str(), a_seqs + a_off[p], rl, filter, &aln, rl / 2 > 15 ? rl / 2 : 15);
+    int32_t *o = out + 5 * p;
+    o[0] = aln.sw_score;
+    o[1] = aln.ref_begin;
+    o[2] = aln.ref_end;
+    o[3] = aln.query_begin;
+    o[4] = aln.query_end;
+  }
+  return 0;
+}
+
 }  // extern "C"

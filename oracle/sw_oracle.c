@@ -525,3 +525,148 @@ int sw_oracle_cigar_batch(const char *a_seqs, const int64_t *a_off, const int32_
   return swo_batch_run(a_seqs, a_off, a_len, b_seqs, b_off, b_len, n, match, mismatch, gap_open, gap_extend, ambiguity,
                        nthreads, out, 6, ops, nops, ops_cap);
 }
+
+/* ---- protein (an nc x nc substitution matrix) ------------------------------------------
+ * The same result rules as sw_oracle_align_codes (score, lexicographically smallest end,
+ * begin by the reversed sweep that stops at the first row reaching the score), with
+ * scores mat[a * nc + b] for codes a (A) and b (B) below nc.  The reference's protein
+ * kernels (src/adept-sw/kernel.cpp:510-899, sequence_aa_kernel / sequence_aa_reverse) take
+ * a 24 x 24 scoring matrix and a 91-entry ASCII encoding from their caller. */
+static void swo_sweep_mat(const uint8_t *A, int M, const uint8_t *B, int N, const int16_t *mat, int nc, int gO, int gE,
+                          int stop_at, int32_t *Hrow, int32_t *Erow, int *best, int *bi, int *bj) {
+  int b = 0, ii = -1, jj = 0;
+  for (int j = 0; j < N; j++) {
+    Hrow[j] = 0;
+    Erow[j] = -gO;
+  }
+  for (int i = 0; i < M; i++) {
+    const int16_t *srow = mat + nc * A[i];
+    int32_t diag = 0, f = -gO;
+    for (int j = 0; j < N; j++) {
+      int32_t e = Erow[j];
+      int32_t h = diag + srow[B[j]];
+      if (e > h) h = e;
+      if (f > h) h = f;
+      if (h < 0) h = 0;
+      diag = Hrow[j];
+      Hrow[j] = h;
+      int32_t hg = h - gO, en = e - gE, fn = f - gE;
+      Erow[j] = en > hg ? en : hg;
+      f = fn > hg ? fn : hg;
+      if (h > b) {
+        b = h;
+        ii = i;
+        jj = j;
+      }
+    }
+    if (stop_at > 0 && b >= stop_at) break;
+  }
+  *best = b;
+  *bi = ii;
+  *bj = jj;
+}
+
+int sw_oracle_align_protein(const uint8_t *A, int M, const uint8_t *B, int N, const int16_t *mat, int nc, int gO, int gE,
+                            int32_t *out) {
+  out[0] = 0;
+  out[1] = -1;
+  out[2] = -1;
+  out[3] = 0;
+  out[4] = 0;
+  if (M <= 0 || N <= 0) return 0;
+  int32_t *work = (int32_t *)malloc(sizeof(int32_t) * 2 * (size_t)N + 16);
+  int S, ie, je;
+  swo_sweep_mat(A, M, B, N, mat, nc, gO, gE, 0, work, work + N, &S, &ie, &je);
+  if (S > 0) {
+    const int Mr = ie + 1, Nr = je + 1;
+    uint8_t *ra = (uint8_t *)malloc((size_t)Mr + (size_t)Nr + 16);
+    uint8_t *rb = ra + Mr;
+    for (int i = 0; i < Mr; i++) ra[i] = A[ie - i];
+    for (int j = 0; j < Nr; j++) rb[j] = B[je - j];
+    int S2, ir, jr;
+    swo_sweep_mat(ra, Mr, rb, Nr, mat, nc, gO, gE, S, work, work + N, &S2, &ir, &jr);
+    free(ra);
+    out[0] = S;
+    out[1] = ie - ir;
+    out[2] = ie;
+    out[3] = je - jr;
+    out[4] = je;
+  }
+  free(work);
+  return 0;
+}
+
+typedef struct {
+  const char *a_seqs, *b_seqs;
+  const int64_t *a_off, *b_off;
+  const int32_t *a_len, *b_len;
+  int64_t n;
+  const int16_t *mat, *enc;
+  int gO, gE;
+  int32_t *out;
+  int64_t next;
+  pthread_mutex_t mu;
+} swo_pbatch;
+
+static void *swo_pworker(void *arg) {
+  swo_pbatch *bt = (swo_pbatch *)arg;
+  uint8_t *ca = NULL, *cb = NULL;
+  int64_t cap_a = 0, cap_b = 0;
+  for (;;) {
+    pthread_mutex_lock(&bt->mu);
+    const int64_t lo = bt->next;
+    bt->next += 64;
+    pthread_mutex_unlock(&bt->mu);
+    if (lo >= bt->n) break;
+    const int64_t hi = lo + 64 < bt->n ? lo + 64 : bt->n;
+    for (int64_t p = lo; p < hi; p++) {
+      const int32_t la = bt->a_len[p], lb = bt->b_len[p];
+      if (la > cap_a) {
+        free(ca);
+        cap_a = la + 64;
+        ca = (uint8_t *)malloc((size_t)cap_a);
+      }
+      if (lb > cap_b) {
+        free(cb);
+        cap_b = lb + 64;
+        cb = (uint8_t *)malloc((size_t)cap_b);
+      }
+      for (int i = 0; i < la; i++) ca[i] = (uint8_t)bt->enc[(unsigned char)bt->a_seqs[bt->a_off[p] + i]];
+      for (int j = 0; j < lb; j++) cb[j] = (uint8_t)bt->enc[(unsigned char)bt->b_seqs[bt->b_off[p] + j]];
+      sw_oracle_align_protein(ca, la, cb, lb, bt->mat, 24, bt->gO, bt->gE, bt->out + 5 * p);
+    }
+  }
+  free(ca);
+  free(cb);
+  return NULL;
+}
+
+/* Protein batch: bytes below 91 encoded by enc (ADEPT's 91-entry table, indices < 24),
+ * mat = 24 x 24 scores; the caller checks the bytes.  out = n x 5 as the DNA batch. */
+int sw_oracle_protein_batch(const char *a_seqs, const int64_t *a_off, const int32_t *a_len, const char *b_seqs,
+                            const int64_t *b_off, const int32_t *b_len, int64_t n, const int16_t *mat,
+                            const int16_t *enc, int gap_open, int gap_extend, int nthreads, int32_t *out) {
+  swo_pbatch bt;
+  bt.a_seqs = a_seqs;
+  bt.b_seqs = b_seqs;
+  bt.a_off = a_off;
+  bt.b_off = b_off;
+  bt.a_len = a_len;
+  bt.b_len = b_len;
+  bt.n = n;
+  bt.mat = mat;
+  bt.enc = enc;
+  bt.gO = gap_open;
+  bt.gE = gap_extend;
+  bt.out = out;
+  bt.next = 0;
+  pthread_mutex_init(&bt.mu, NULL);
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 512) nthreads = 512;
+  pthread_t th[512];
+  for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, swo_pworker, &bt);
+  swo_pworker(&bt);
+  for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+  pthread_mutex_destroy(&bt.mu);
+  return 0;
+}

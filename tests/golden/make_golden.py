@@ -163,6 +163,51 @@ def main() -> None:
          "result_layout": "score, a_begin, a_end, b_begin, b_end",
          "scorings": {k: list(v) for k, v in SCORINGS.items()}, "pairs": rec}))
     print(f"{len(cases)} known-answer cases, {len(rec)} sample pairs")
+    make_protein(oracle, Pairs)
+
+
+def make_protein(oracle, Pairs) -> None:
+    """ssw_protein_samples.json: seeded protein pairs (random, and mutated copies with
+    indels and flanks) with a seeded symmetric 24 x 24 matrix (diagonal 4..11, elsewhere
+    -4..3) and the 24-letter encoding, and the reference SSW's outputs (Aligner with that
+    matrix and translation, SetGapPenalty) under three gap settings."""
+    import numpy as np
+
+    rng = np.random.default_rng(2024)
+    m = rng.integers(-4, 4, (24, 24))
+    m = np.triu(m) + np.triu(m, 1).T
+    np.fill_diagonal(m, rng.integers(4, 12, 24))
+    enc = oracle.protein_encoding()
+    letters = oracle.PROTEIN_LETTERS
+    a, b = [], []
+    for k in range(240):
+        x = "".join(rng.choice(list(letters[:20]) + ["B", "Z", "X", "*"], rng.integers(1, 600)))
+        if k % 4 == 0:
+            y = "".join(rng.choice(list(letters), rng.integers(1, 500)))
+        else:
+            y = []
+            for ch in x:
+                r = rng.random()
+                if r < 0.03:
+                    continue
+                if r < 0.06:
+                    y.append("".join(rng.choice(list(letters[:20]), rng.integers(1, 4))))
+                y.append(ch if rng.random() > 0.15 else rng.choice(list(letters)))
+            y = "".join(rng.choice(list(letters[:20]), rng.integers(0, 50))) + "".join(y) + "A"
+        a.append(x)
+        b.append(y)
+    pairs = Pairs.from_lists(a, b)
+    gaps = [[11, 1], [10, 2], [5, 2]]
+    rec = {"matrix": m.astype(int).tolist(), "encoding": enc.astype(int).tolist(), "gaps": gaps,
+           "pairs": [{"a": x, "b": y} for x, y in zip(a, b)]}
+    for go, ge in gaps:
+        out = oracle.ref_protein_batch(pairs, m.astype(np.int16), enc, go, ge)
+        for r, o in zip(rec["pairs"], out.tolist()):
+            r.setdefault("reference", {})[f"{go}/{ge}"] = o
+    rec["source"] = ("reference SSW (src/ssw) as Aligner(matrix, 24, translation, 128) + SetGapPenalty; "
+                     "A = SSW ref, B = SSW query")
+    (HERE / "ssw_protein_samples.json").write_text(json.dumps(rec))
+    print(f"{len(a)} protein pairs")
 
 
 if __name__ == "__main__":

@@ -251,3 +251,40 @@ def test_equal_gap_penalties_are_outside_the_contract():
     assert (got[:, 0] >= want[:, 0]).all()
     assert (got[:, 0] > want[:, 0]).any()
     assert np.array_equal(oracle.align_batch(pairs, (2, 2, 3, 2, 2)), oracle.ref_align_batch(pairs, (2, 2, 3, 2, 2)))
+
+
+# ---- protein ---------------------------------------------------------------------------
+
+PROT = json.loads((GOLDEN / "ssw_protein_samples.json").read_text())
+
+
+@pytest.mark.parametrize("gaps", PROT["gaps"])
+def test_protein_oracle_vs_recorded_reference(gaps):
+    """The protein restatement against the reference SSW's recorded outputs (a seeded
+    24 x 24 matrix, 240 pairs incl. unrelated and mutated ones)."""
+    recs = PROT["pairs"]
+    pairs = Pairs.from_lists([r["a"] for r in recs], [r["b"] for r in recs])
+    out = oracle.protein_batch(pairs, np.array(PROT["matrix"], np.int16), np.array(PROT["encoding"], np.int16),
+                               *gaps)
+    want = np.array([r["reference"][f"{gaps[0]}/{gaps[1]}"] for r in recs], dtype=np.int32)
+    assert np.array_equal(out, want)
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference SSW not built (needs the reference checkout)")
+def test_protein_oracle_vs_live_reference():
+    rng = random.Random(7)
+    letters = oracle.PROTEIN_LETTERS
+    a, b = [], []
+    for k in range(1500):
+        x = "".join(rng.choice(letters) for _ in range(rng.randint(1, 300)))
+        y = x[rng.randint(0, len(x) - 1):] if k % 2 else "".join(rng.choice(letters) for _ in range(rng.randint(1, 300)))
+        a.append(x)
+        b.append(y + rng.choice(letters))
+    pairs = Pairs.from_lists(a, b)
+    nr = np.random.default_rng(5)
+    m = nr.integers(-3, 3, (24, 24))
+    m = (np.triu(m) + np.triu(m, 1).T).astype(np.int16)
+    np.fill_diagonal(m, nr.integers(3, 9, 24))
+    enc = oracle.protein_encoding()
+    for go, ge in ((11, 1), (7, 3), (4, 1)):
+        assert np.array_equal(oracle.protein_batch(pairs, m, enc, go, ge), oracle.ref_protein_batch(pairs, m, enc, go, ge))
