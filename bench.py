@@ -312,7 +312,7 @@ def _protein_path(n: int = 100_000) -> dict:
     """Protein alignment (mhsw_align_protein, host arrays in and out) with a seeded 24 x 24
     matrix (diagonal 4..11, elsewhere -4..3), gaps 11/1; 1 warm-up call, 3 timed (wall
     clock, synchronous call).  GCUPS count the forward cells.  Beside it the oracle port
-    on the first 2,000 pairs."""
+    on the first 20,000 pairs."""
     from mhm2_staging_gb300 import GPUDriver
     from oracle import oracle
 
@@ -330,7 +330,7 @@ def _protein_path(n: int = 100_000) -> dict:
         d.align_protein(pairs, m, enc)
     dt = (time.perf_counter() - t0) / 3
     cells = float(pairs.cells())
-    sub = pairs.slice(0, 2000)
+    sub = pairs.slice(0, 20_000)
     t0 = time.perf_counter()
     oracle.protein_batch(sub, m, enc, 11, 1, os.cpu_count() or 1)
     cdt = time.perf_counter() - t0

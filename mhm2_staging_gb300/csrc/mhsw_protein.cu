@@ -311,7 +311,9 @@ int mhsw_align_protein(mhsw_driver *d, const mhsw_pairs *pairs, const int16_t *s
   A(&bad, 1);
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t warps = std::min<int64_t>(n, (int64_t)sms * 16);
+  // one warp per pair at a time; 24 resident warps per SM (76 registers x 128 threads
+  // fits 6 blocks of 4 warps) to cover the row chain's latency
+  const int64_t warps = std::min<int64_t>(n, (int64_t)sms * 24);
   A(&rows, (size_t)(warps * max_n));
   if (!host_io) {
     o5 = out5;
