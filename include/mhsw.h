@@ -221,6 +221,18 @@ int mhsw_get_aln_results(mhsw_driver *drv, mhsw_aln_results *out);
  * out5[5*i .. 5*i+4] = score, a_begin, a_end, b_begin, b_end (SSW ref = A,
  * SSW query = B; score 0 gives -1, -1, 0, 0 as SSW does). */
 int mhsw_align_pairs(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form);
+/* mhsw_align_pairs in two halves, for callers that overlap one batch's copies with
+ * another's work (klign overlaps its blocks the same way, src/klign.cpp:552-606): the
+ * first enqueues the whole call -- copies in, kernels, the copy of out5 -- and returns;
+ * mhsw_align_wait completes every call still pending (errors, timing, CIGAR rounds) and
+ * must come before their out5 are read.  A handle keeps up to two host batches in flight
+ * on two device input sets: a batch's copies wait only for the call two back, so they run
+ * while the previous call's kernels do (kernels stay in call order); a third call first
+ * completes the oldest.  Host arrays and out5 stay untouched by the caller until completed,
+ * and should be pinned for the copies to run asynchronously.  In score2 or CIGAR mode, for
+ * device batches, and on any other call on the handle, pending calls complete first. */
+int mhsw_align_pairs_async(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form);
+int mhsw_align_wait(mhsw_driver *drv);
 int mhsw_last_timing(mhsw_driver *drv, mhsw_timing *out);
 
 /* ---- serving form (no counterpart in the reference) ------------------------ */

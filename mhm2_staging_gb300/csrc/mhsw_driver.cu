@@ -131,6 +131,31 @@ struct mhsw_driver {
   DBuf<unsigned char> c_pool, c_temp;
   HBuf<int> h_ccounts;
   cudaEvent_t ev_c[2] = {nullptr, nullptr};
+  // Batch calls enqueued (mhsw_align_pairs_async) and not yet completed: up to two, in
+  // two slots used in turn.  A host batch copies into its slot's input set on the copy
+  // streams, which wait only for that set's previous call (two calls back), so its copies
+  // run while the previous call's kernels do; kernels stay in order on the handle's stream.
+  struct Pending {
+    bool active = false;
+    int64_t n = 0;
+    double cells = 0;
+    uint64_t seq = 0;
+    mhsw::PairSet ps;
+  } pend[2];
+  struct InSet {
+    DBuf<char> a_seq, b_seq;
+    DBuf<int64_t> a_off, b_off;
+    DBuf<int32_t> a_len, b_len;
+    cudaEvent_t free_ev = nullptr;  // recorded after the kernels of the set's last call
+    bool used = false;
+  } in_sets[2];
+  static constexpr int kCopyStreams = 4;
+  cudaStream_t copy_st[kCopyStreams] = {};
+  cudaEvent_t copy_ev[kCopyStreams] = {};
+  cudaEvent_t ev_p[2][5] = {};  // per slot: phase events of its call
+  HBuf<int> h_counts_p[2];       // per slot: the call's counters
+  int next_slot = 0;
+  uint64_t call_seq = 0;
 
   // CUDA graph of a device-resident batch: captured the second time the same batch
   // (same pointers, sizes and settings) is aligned, replayed from then on.
@@ -233,6 +258,23 @@ struct mhsw_driver {
     h_ccounts.release();
     for (auto &e : ev_c)
       if (e) cudaEventDestroy(e);
+    for (auto &in : in_sets) {
+      in.a_seq.release();
+      in.b_seq.release();
+      in.a_off.release();
+      in.b_off.release();
+      in.a_len.release();
+      in.b_len.release();
+      if (in.free_ev) cudaEventDestroy(in.free_ev);
+    }
+    for (auto &c : copy_st)
+      if (c) cudaStreamDestroy(c);
+    for (auto &e : copy_ev)
+      if (e) cudaEventDestroy(e);
+    for (auto &row : ev_p)
+      for (auto &e : row)
+        if (e) cudaEventDestroy(e);
+    for (auto &h : h_counts_p) h.release();
     h_a.release();
     h_b.release();
     h_aoff.release();
@@ -257,6 +299,8 @@ struct mhsw_driver {
   } while (0)
 
 namespace {
+
+int finish_pending(mhsw_driver *d);
 
 // Device buffers for n pairs and the byte totals; result arrays; lists.
 int ensure_device(mhsw_driver *d, int64_t n, int64_t a_bytes, int64_t b_bytes) {
@@ -673,29 +717,44 @@ mhsw::PairSet staged_pairs(mhsw_driver *d) {
   return ps;
 }
 
-// Host-to-device copy of the two sequence arenas, split into pieces issued on the side
-// streams so several copy engines move them at once; the main stream waits for all.
-int copy_in_parallel(mhsw_driver *d, char *da, const char *ha, size_t na, char *db, const char *hb, size_t nb) {
+// A host batch into input set `in`: arenas in 64 MB pieces and the offsets and lengths,
+// spread over the copy streams; the handle's stream waits for all of them.  after_free:
+// the copy streams wait only for the set's previous call (its free event), not for the
+// work on the handle's stream, so the copies overlap the previous call's kernels;
+// otherwise they wait for everything issued on the handle's stream so far.
+int copy_batch_in(mhsw_driver *d, mhsw_driver::InSet &in, const mhsw_pairs *pairs, int64_t n, int64_t ta,
+                  int64_t tb, bool after_free) {
   constexpr size_t kPiece = size_t(64) << 20;
-  if (na + nb <= 2 * kPiece) {
-    MHSW_CK(cudaMemcpyAsync(da, ha, na, cudaMemcpyHostToDevice, d->st), "H2D");
-    MHSW_CK(cudaMemcpyAsync(db, hb, nb, cudaMemcpyHostToDevice, d->st), "H2D");
-    return MHSW_OK;
-  }
-  constexpr int kLanes = 4;
-  MHSW_CK(mhsw::fork_to(d->forks, d->st, kLanes), "fork copies");
-  int lane = 0;
-  for (int which = 0; which < 2; which++) {
-    char *dst = which ? db : da;
-    const char *src = which ? hb : ha;
-    const size_t len = which ? nb : na;
-    for (size_t o = 0; o < len; o += kPiece) {
-      const size_t k = std::min(kPiece, len - o);
-      MHSW_CK(cudaMemcpyAsync(dst + o, src + o, k, cudaMemcpyHostToDevice, d->forks.side[lane]), "H2D");
-      lane = (lane + 1) % kLanes;
+  constexpr int kLanes = mhsw_driver::kCopyStreams;
+  if (!after_free) MHSW_CK(cudaEventRecord(d->copy_ev[0], d->st), "event");
+  for (int k = 0; k < kLanes; k++) {
+    if (after_free) {
+      if (in.used) MHSW_CK(cudaStreamWaitEvent(d->copy_st[k], in.free_ev, 0), "wait input set");
+    } else {
+      MHSW_CK(cudaStreamWaitEvent(d->copy_st[k], d->copy_ev[0], 0), "wait stream");
     }
   }
-  MHSW_CK(mhsw::join_from(d->forks, d->st, kLanes), "join copies");
+  int lane = 0;
+  auto put = [&](void *dst, const void *src, size_t len) -> cudaError_t {
+    for (size_t o = 0; o < len; o += kPiece) {
+      const size_t k = std::min(kPiece, len - o);
+      cudaError_t e = cudaMemcpyAsync(static_cast<char *>(dst) + o, static_cast<const char *>(src) + o, k,
+                                      cudaMemcpyHostToDevice, d->copy_st[lane]);
+      if (e) return e;
+      lane = (lane + 1) % kLanes;
+    }
+    return cudaSuccess;
+  };
+  MHSW_CK(put(in.a_seq.p, pairs->a_seq, (size_t)ta), "H2D");
+  MHSW_CK(put(in.b_seq.p, pairs->b_seq, (size_t)tb), "H2D");
+  MHSW_CK(put(in.a_off.p, pairs->a_off, sizeof(int64_t) * n), "H2D");
+  MHSW_CK(put(in.b_off.p, pairs->b_off, sizeof(int64_t) * n), "H2D");
+  MHSW_CK(put(in.a_len.p, pairs->a_len, sizeof(int32_t) * n), "H2D");
+  MHSW_CK(put(in.b_len.p, pairs->b_len, sizeof(int32_t) * n), "H2D");
+  for (int k = 0; k < kLanes; k++) {
+    MHSW_CK(cudaEventRecord(d->copy_ev[k], d->copy_st[k]), "event");
+    MHSW_CK(cudaStreamWaitEvent(d->st, d->copy_ev[k], 0), "wait copies");
+  }
   return MHSW_OK;
 }
 
@@ -812,6 +871,11 @@ int mhsw_driver_init(mhsw_driver *d, int rank_me, int rank_n, short match_score,
   MHSW_CK(mhsw::forks_create(d->forks), "side streams");
   for (auto &e : d->ev_t) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
   for (auto &e : d->ev_c) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
+  for (auto &row : d->ev_p)
+    for (auto &e : row) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
+  for (auto &in : d->in_sets) MHSW_CK(cudaEventCreateWithFlags(&in.free_ev, cudaEventDisableTiming), "cudaEventCreate");
+  for (auto &c : d->copy_st) MHSW_CK(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking), "cudaStreamCreate");
+  for (auto &e : d->copy_ev) MHSW_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
   MHSW_CK(cudaDeviceGetAttribute(&d->sms, cudaDevAttrMultiProcessorCount, d->device), "device attribute");
   d->sc = s;
   d->inited = true;
@@ -883,6 +947,7 @@ int mhsw_run_kernel_forwards(mhsw_driver *d, const char *const *reads, const int
   int rc = ready(d);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
   if (n < 0 || (n > 0 && (!reads || !read_lens || !contigs || !contig_lens)))
     return d->fail(MHSW_ERR_ARG, "bad batch arguments");
   for (int32_t i = 0; i < n; i++)
@@ -945,6 +1010,7 @@ int mhsw_run_kernel_backwards(mhsw_driver *d, const char *const *reads, const in
   int rc = ready(d);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
   (void)reads;
   (void)read_lens;
   (void)contigs;
@@ -1066,10 +1132,71 @@ int mhsw_get_aln_results(mhsw_driver *d, mhsw_aln_results *out) {
   return MHSW_OK;
 }
 
-int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form) {
-  int rc = ready(d);
+}  // extern "C"
+
+namespace {
+
+// Completes the pending batch call of a slot, if any (the caller holds d->mu): waits for
+// its stream work, surfaces asynchronous faults, runs the CIGAR pass's host-driven rounds
+// and records the timing.
+int finish_slot(mhsw_driver *d, int s) {
+  mhsw_driver::Pending &pd = d->pend[s];
+  if (!pd.active) return MHSW_OK;
+  pd.active = false;
+  const int64_t n = pd.n;
+  cudaEvent_t *ev = d->ev_p[s];
+  MHSW_CK(cudaEventSynchronize(ev[4]), "sync");
+  // Surface any asynchronous kernel fault as an error status.
+  MHSW_CK(cudaGetLastError(), "kernel execution");
+  d->cigar_ms = 0;
+  d->cigar_generic = 0;
+  if (n > 0 && d->cigar) {
+    const int rc = finish_cigar(d, pd.ps);
+    if (rc) return rc;
+  }
+  const int *hc = d->h_counts_p[s].p;
+  d->timing.fwd_ms = elapsed(ev[1], ev[2]);
+  d->timing.rev_ms = elapsed(ev[2], ev[3]);
+  d->timing.total_ms = elapsed(ev[0], ev[4]);
+  d->timing.fwd_cells = pd.cells;
+  d->timing.n_pairs = n;
+  d->timing.n_overflow16 = n > 0 && hc ? hc[0] : 0;
+  d->timing.n_rev_wide = n > 0 && hc ? hc[1] : 0;
+  d->timing.launches = d->launches;
+  d->timing.graph_replays = d->graph_launches;
+  d->timing.cigar_ms = d->cigar_ms;
+  d->timing.n_cigar_generic = d->cigar_generic;
+  return MHSW_OK;
+}
+
+// Completes every pending batch call, oldest first.
+int finish_pending(mhsw_driver *d) {
+  const bool both = d->pend[0].active && d->pend[1].active;
+  const int first = both ? (d->pend[0].seq < d->pend[1].seq ? 0 : 1) : (d->pend[0].active ? 0 : 1);
+  int rc = finish_slot(d, first);
   if (rc) return rc;
-  std::lock_guard<std::mutex> lk(d->mu);
+  return finish_slot(d, 1 - first);
+}
+
+// Everything of a batch call up to its completion event, enqueued on the handle's stream;
+// leaves the call pending (finish_pending completes it).
+int align_pairs_begin(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form) {
+  // Host batches take the slots in turn and overlap; score2 and CIGAR outputs live in one
+  // set of buffers, and device batches may be captured into a graph with slot 0's events,
+  // so those complete everything pending first and use slot 0.
+  const bool overlap = host_io && !d->score2 && !d->cigar;
+  int slot = 0;
+  int rc = MHSW_OK;
+  if (overlap) {
+    slot = d->next_slot;
+    d->next_slot ^= 1;
+    rc = finish_slot(d, slot);
+  } else {
+    rc = finish_pending(d);
+    d->next_slot = 1;
+  }
+  if (rc) return rc;
+  cudaEvent_t *ev = d->ev_p[slot];
   if (!pairs || pairs->n < 0 || (pairs->n > 0 && !out5)) return d->fail(MHSW_ERR_ARG, "bad pairs");
   if (form != MHSW_FORM_PLAIN && form != MHSW_FORM_BATCHED) return d->fail(MHSW_ERR_ARG, "unknown form %d", form);
   if (d->ev_live) MHSW_CK(cudaEventSynchronize(d->ev_done), "wait previous batch");
@@ -1081,7 +1208,7 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
   double cells = 0;
   int64_t ta = 0, tb = 0;
   mhsw::PairSet ps;
-  MHSW_CK(cudaEventRecord(d->ev_t[0], d->st), "event");
+  MHSW_CK(cudaEventRecord(ev[0], d->st), "event");
   const bool hinted_sizes =
       pairs->max_a_len > 0 && pairs->max_b_len > 0 && pairs->a_bytes > 0 && pairs->b_bytes > 0;
   if (host_io) {
@@ -1103,20 +1230,23 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
         cells += (double)la * (double)lb;
       }
     }
-    rc = ensure_device(d, n, ta, tb);
-    if (rc) return rc;
-    rc = copy_in_parallel(d, d->a_seq.p, pairs->a_seq, (size_t)ta, d->b_seq.p, pairs->b_seq, (size_t)tb);
-    if (rc) return rc;
-    MHSW_CK(cudaMemcpyAsync(d->a_off.p, pairs->a_off, sizeof(int64_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
-    MHSW_CK(cudaMemcpyAsync(d->b_off.p, pairs->b_off, sizeof(int64_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
-    MHSW_CK(cudaMemcpyAsync(d->a_len.p, pairs->a_len, sizeof(int32_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
-    MHSW_CK(cudaMemcpyAsync(d->b_len.p, pairs->b_len, sizeof(int32_t) * n, cudaMemcpyHostToDevice, d->st), "H2D");
-    ps.a_seq = d->a_seq.p;
-    ps.a_off = d->a_off.p;
-    ps.a_len = d->a_len.p;
-    ps.b_seq = d->b_seq.p;
-    ps.b_off = d->b_off.p;
-    ps.b_len = d->b_len.p;
+    mhsw_driver::InSet &in = d->in_sets[slot];
+    MHSW_CK(in.a_seq.reserve((size_t)ta + 16), "cudaMalloc A");
+    MHSW_CK(in.b_seq.reserve((size_t)tb + 16), "cudaMalloc B");
+    MHSW_CK(in.a_off.reserve((size_t)n + 1), "cudaMalloc offsets");
+    MHSW_CK(in.b_off.reserve((size_t)n + 1), "cudaMalloc offsets");
+    MHSW_CK(in.a_len.reserve((size_t)n + 1), "cudaMalloc lengths");
+    MHSW_CK(in.b_len.reserve((size_t)n + 1), "cudaMalloc lengths");
+    if (n > 0) {
+      rc = copy_batch_in(d, in, pairs, n, ta, tb, overlap);
+      if (rc) return rc;
+    }
+    ps.a_seq = in.a_seq.p;
+    ps.a_off = in.a_off.p;
+    ps.a_len = in.a_len.p;
+    ps.b_seq = in.b_seq.p;
+    ps.b_off = in.b_off.p;
+    ps.b_len = in.b_len.p;
   } else if (hinted_sizes) {
     // device-resident inputs with size hints: no host round trip
     ma = pairs->max_a_len;
@@ -1163,6 +1293,7 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
     MHSW_CK(d->a_code.reserve((size_t)ta + 16), "cudaMalloc codes");
     MHSW_CK(d->b_code.reserve((size_t)tb + 16), "cudaMalloc codes");
     MHSW_CK(d->h_counts.reserve(4), "cudaMallocHost");
+    MHSW_CK(d->h_counts_p[slot].reserve(4), "cudaMallocHost");
     if (host_io) MHSW_CK(d->out5.reserve((size_t)n * 5), "cudaMalloc out5");
   }
   rc = attach_score2(d, &ps, n, ta);
@@ -1184,17 +1315,17 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
       int r = translate_batch(d, &ps, ta, tb);
       if (r) return r;
     }
-    MHSW_CK(mark(d->ev_t[1]), "event");
+    MHSW_CK(mark(ev[1]), "event");
     if (n > 0) {
       int r = forward_any(d, ps, ma, mb, form);
       if (r) return r;
     }
-    MHSW_CK(mark(d->ev_t[2]), "event");
+    MHSW_CK(mark(ev[2]), "event");
     if (n > 0) {
       int r = run_reverse(d, ps, ma, mb, d->fwd_order);
       if (r) return r;
     }
-    MHSW_CK(mark(d->ev_t[3]), "event");
+    MHSW_CK(mark(ev[3]), "event");
     if (n > 0 && d->cigar) {
       MHSW_CK(mark(d->ev_c[0]), "event");
       int r = enqueue_cigar(d, ps);
@@ -1209,7 +1340,8 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
         MHSW_CK(mhsw::launch_pack5(result_set(d), n, out5, d->st), "pack5");
       }
       d->launches += 1;
-      MHSW_CK(cudaMemcpyAsync(d->h_counts.p, d->l_counts.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->st), "D2H");
+      MHSW_CK(cudaMemcpyAsync(d->h_counts_p[slot].p, d->l_counts.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, d->st),
+              "D2H");
     }
     return MHSW_OK;
   };
@@ -1285,33 +1417,51 @@ int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int
     rc = enqueue();
     if (rc) return rc;
   }
-  MHSW_CK(cudaEventRecord(d->ev_t[4], d->st), "event");
-  MHSW_CK(cudaEventSynchronize(d->ev_t[4]), "sync");
-  // Surface any asynchronous kernel fault as an error status.
-  MHSW_CK(cudaGetLastError(), "kernel execution");
-  d->cigar_ms = 0;
-  d->cigar_generic = 0;
-  if (n > 0 && d->cigar) {
-    rc = finish_cigar(d, ps);
-    if (rc) return rc;
+  MHSW_CK(cudaEventRecord(ev[4], d->st), "event");
+  if (host_io) {
+    // the slot's input set is free again once this call's kernels are done
+    MHSW_CK(cudaEventRecord(d->in_sets[slot].free_ev, d->st), "event");
+    d->in_sets[slot].used = true;
   }
-  d->timing.fwd_ms = elapsed(d->ev_t[1], d->ev_t[2]);
-  d->timing.rev_ms = elapsed(d->ev_t[2], d->ev_t[3]);
-  d->timing.total_ms = elapsed(d->ev_t[0], d->ev_t[4]);
-  d->timing.fwd_cells = cells;
-  d->timing.n_pairs = n;
-  d->timing.n_overflow16 = n > 0 ? d->h_counts.p[0] : 0;
-  d->timing.n_rev_wide = n > 0 ? d->h_counts.p[1] : 0;
-  d->timing.launches = d->launches;
-  d->timing.graph_replays = d->graph_launches;
-  d->timing.cigar_ms = d->cigar_ms;
-  d->timing.n_cigar_generic = d->cigar_generic;
+  mhsw_driver::Pending &pd = d->pend[slot];
+  pd.active = true;
+  pd.n = n;
+  pd.cells = cells;
+  pd.seq = ++d->call_seq;
+  pd.ps = ps;
   return MHSW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mhsw_align_pairs(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form) {
+  int rc = ready(d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(d->mu);
+  rc = align_pairs_begin(d, pairs, out5, host_io, form);
+  if (rc) return rc;
+  return finish_pending(d);
+}
+
+int mhsw_align_pairs_async(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form) {
+  int rc = ready(d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(d->mu);
+  return align_pairs_begin(d, pairs, out5, host_io, form);
+}
+
+int mhsw_align_wait(mhsw_driver *d) {
+  if (!d) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  return finish_pending(d);
 }
 
 int mhsw_last_timing(mhsw_driver *d, mhsw_timing *out) {
   if (!d || !out) return MHSW_ERR_ARG;
   std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
   *out = d->timing;
   return MHSW_OK;
 }
@@ -1319,6 +1469,7 @@ int mhsw_last_timing(mhsw_driver *d, mhsw_timing *out) {
 int mhsw_driver_set_score2(mhsw_driver *d, int on) {
   if (!d) return MHSW_ERR_ARG;
   std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
   d->score2 = on != 0;
   return MHSW_OK;
 }
@@ -1327,6 +1478,7 @@ int mhsw_last_score2(mhsw_driver *d, int32_t *score2, int32_t *a_end2, int host_
   int rc = ready(d);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
   const int64_t n = d->score2_n;
   if (n < 0 || !d->r_score2.p) return d->fail(MHSW_ERR_STATE, "score2 mode was off for the last batch");
   if (n > 0 && (!score2 || !a_end2)) return d->fail(MHSW_ERR_ARG, "NULL output");
@@ -1341,6 +1493,7 @@ int mhsw_last_score2(mhsw_driver *d, int32_t *score2, int32_t *a_end2, int host_
 int mhsw_driver_set_cigar(mhsw_driver *d, int on) {
   if (!d) return MHSW_ERR_ARG;
   std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
   d->cigar = on != 0;
   return MHSW_OK;
 }
@@ -1350,6 +1503,7 @@ int mhsw_last_cigar(mhsw_driver *d, int32_t *nops, int32_t *mismatches, int64_t 
   int rc = ready(d);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
   const int64_t n = d->cigar_n;
   if (n < 0) return d->fail(MHSW_ERR_STATE, "no CIGARs: CIGAR mode was off for the last batch, or it has not completed");
   if (n == 0) {
@@ -1425,6 +1579,7 @@ int align_resident(mhsw_driver *d, const PairSet &in, int64_t a_bytes, int max_a
   int rc = ready(d);
   if (rc) return rc;
   std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
   if (form != MHSW_FORM_PLAIN && form != MHSW_FORM_BATCHED) return d->fail(MHSW_ERR_ARG, "unknown form %d", form);
   if (d->ev_live) MHSW_CK(cudaEventSynchronize(d->ev_done), "wait previous batch");
   d->ev_live = false;

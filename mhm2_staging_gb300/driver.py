@@ -174,6 +174,8 @@ SIGNATURES: dict[str, tuple] = {
     "mhsw_kernel_block": (C.c_int, [_P]),
     "mhsw_get_aln_results": (C.c_int, [_P, C.POINTER(_AlnResults)]),
     "mhsw_align_pairs": (C.c_int, [_P, C.POINTER(PairsT), _P, C.c_int, C.c_int]),
+    "mhsw_align_pairs_async": (C.c_int, [_P, C.POINTER(PairsT), _P, C.c_int, C.c_int]),
+    "mhsw_align_wait": (C.c_int, [_P]),
     "mhsw_last_timing": (C.c_int, [_P, C.POINTER(Timing)]),
     "mhsw_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P), C.c_char_p, C.c_size_t]),
     "mhsw_server_destroy": (None, [_P]),
@@ -483,6 +485,29 @@ class GPUDriver:
         self._ck(self._lib.mhsw_align_pairs(self._h, C.byref(pt), out.ctypes.data_as(_P) if n else None, 1, form),
                  "align_pairs")
         return out
+
+    def align_pairs_async(self, pairs: "Pairs", form: int = FORM_PLAIN, out: np.ndarray | None = None,
+                          hints: bool = False) -> np.ndarray:
+        """align_pairs enqueued without waiting (mhsw_align_pairs_async): returns the output
+        array, valid after wait().  pairs and out are kept referenced until then; pinned
+        host arrays let the copies overlap other work."""
+        n = pairs.n
+        if out is None:
+            out = np.zeros((n, 5), dtype=np.int32)
+        pt = pairs.c_struct()
+        if hints:
+            pt.max_a_len, pt.max_b_len, pt.cells, pt.a_bytes, pt.b_bytes = pairs.extents()
+        self._pending = (pairs, out, pt)
+        self._ck(self._lib.mhsw_align_pairs_async(self._h, C.byref(pt), out.ctypes.data_as(_P) if n else None, 1,
+                                                  form), "align_pairs_async")
+        return out
+
+    def wait(self) -> None:
+        """Completes the batch enqueued by align_pairs_async (mhsw_align_wait)."""
+        try:
+            self._ck(self._lib.mhsw_align_wait(self._h), "align_wait")
+        finally:
+            self._pending = None
 
     def align_pairs_device(self, dev: "DevicePairs", out_dev_ptr: int, form: int = FORM_PLAIN) -> None:
         """Aligns pairs already resident on the device (pointers from DevicePairs);

@@ -145,3 +145,53 @@ def test_host_batch_with_stated_extents(gpu):
     want = oracle.align_batch(pairs, SC)
     got = gpu.align_pairs(pairs, form=FORM_BATCHED, hints=True)
     assert not _diff(got, want, pairs)
+
+
+def test_async_halves_alternating_handles(built):
+    """mhsw_align_pairs_async / mhsw_align_wait on two handles in turn (one batch's copies
+    overlapping the other's kernels): every batch gives the oracle's results; a later call
+    on a handle completes its pending batch first."""
+    batches = [workloads.generate(cfg, n=n, first=100 + k) for k, (cfg, n) in
+               enumerate([(2, 20000), (1, 15000), (2, 20000), (0, 10000), (4, 200)])]
+    handles = []
+    for _ in range(2):
+        d = GPUDriver()
+        d.init(0, 1, 1, -3, -5, -2, 0)
+        d.set_ambiguity(-2)
+        handles.append(d)
+    outs = [None] * len(batches)
+    pending = [None, None]
+    for k, b in enumerate(batches):
+        h = k % 2
+        if pending[h] is not None:
+            handles[h].wait()
+        outs[k] = handles[h].align_pairs_async(b, form=FORM_BATCHED, hints=True)
+        pending[h] = k
+    for h in range(2):
+        handles[h].wait()
+    for k, b in enumerate(batches):
+        assert not _diff(outs[k], oracle.align_batch(b, SC), b), f"batch {k}"
+    # a pending batch is completed by the next call on its handle
+    o = handles[0].align_pairs_async(batches[3], form=FORM_PLAIN)
+    assert handles[0].last_timing()["n_pairs"] == batches[3].n
+    assert not _diff(o, oracle.align_batch(batches[3], SC), batches[3])
+    handles[0].wait()  # nothing pending: a no-op
+
+
+def test_async_calls_in_flight_on_one_handle(built):
+    """Several host batches enqueued back to back on one handle (two in flight, the
+    copies of one overlapping the other's kernels): every result matches the oracle."""
+    batches = [workloads.generate(cfg, n=n, first=300 + k) for k, (cfg, n) in
+               enumerate([(2, 30000), (1, 10000), (2, 30000), (0, 10000), (2, 5000), (1, 1)])]
+    d = GPUDriver()
+    d.init(0, 1, 1, -3, -5, -2, 0)
+    d.set_ambiguity(-2)
+    outs = [d.align_pairs_async(b, form=FORM_BATCHED, hints=True) for b in batches]
+    d.wait()
+    for k, b in enumerate(batches):
+        assert not _diff(outs[k], oracle.align_batch(b, SC), b), f"batch {k}"
+    # plain form and unhinted batches go the same way
+    outs = [d.align_pairs_async(b, form=FORM_PLAIN) for b in batches[:3]]
+    d.wait()
+    for k, b in enumerate(batches[:3]):
+        assert not _diff(outs[k], oracle.align_batch(b, SC), b), f"plain batch {k}"
