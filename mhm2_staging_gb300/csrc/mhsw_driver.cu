@@ -1610,6 +1610,28 @@ int align_resident(mhsw_driver *d, const PairSet &in, int64_t a_bytes, int max_a
 void *driver_stream(mhsw_driver *d) { return d ? static_cast<void *>(d->st) : nullptr; }
 int driver_device(mhsw_driver *d) { return d ? d->device : -1; }
 int driver_form(mhsw_driver *d) { return d ? d->form : MHSW_FORM_PLAIN; }
+bool driver_cigar(mhsw_driver *d) { return d && d->cigar; }
+const uint8_t *driver_a_codes(mhsw_driver *d) { return d ? d->a_code.p : nullptr; }
+
+int cigar_resident(mhsw_driver *d, const PairSet &ps) {
+  int rc = ready(d);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (!d->cigar) return d->fail(MHSW_ERR_STATE, "CIGAR mode is off");
+  d->cigar_n = -1;
+  if (ps.n <= 0) {
+    d->cigar_n = 0;
+    return MHSW_OK;
+  }
+  rc = ensure_cigar(d, ps.n);
+  if (rc) return rc;
+  MHSW_CK(cudaEventRecord(d->ev_c[0], d->st), "event");
+  rc = enqueue_cigar(d, ps);
+  if (rc) return rc;
+  MHSW_CK(cudaEventRecord(d->ev_c[1], d->st), "event");
+  MHSW_CK(cudaStreamSynchronize(d->st), "sync");
+  return finish_cigar(d, ps);
+}
 int driver_match(mhsw_driver *d) { return d ? d->sc.match : 1; }
 void driver_gaps(mhsw_driver *d, int *gap_open, int *gap_extend) {
   *gap_open = d ? d->sc.gap_open : 0;

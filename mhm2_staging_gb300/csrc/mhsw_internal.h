@@ -25,6 +25,13 @@ int driver_form(mhsw_driver *d);
 int driver_match(mhsw_driver *d);
 // The handle's gap penalties as positive magnitudes.
 void driver_gaps(mhsw_driver *d, int *gap_open, int *gap_extend);
+// CIGAR mode: runs the CIGAR pass over the batch of the last align_resident call (after
+// its stream work; synchronous); its CIGARs are then what mhsw_last_cigar returns.
+// Returns MHSW_ERR_STATE when the handle is not in CIGAR mode.
+int cigar_resident(mhsw_driver *d, const PairSet &ps);
+bool driver_cigar(mhsw_driver *d);
+// The A codes the last align_resident call translated (device).
+const uint8_t *driver_a_codes(mhsw_driver *d);
 // Second-best scores (device, n entries) of the last align_resident call when the handle
 // is in score2 mode, else null.
 const int32_t *driver_score2(mhsw_driver *d, int64_t n);

@@ -353,6 +353,12 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
     if (!e) {
       rc = mhsw::align_resident(d, ps, rbytes, h_counts[1], h_counts[2], mhsw::driver_form(d), out5);
       if (!rc) s2 = mhsw::driver_score2(d, m);
+      // CIGAR mode: SSW's CIGARs of the aligned candidates (the pair set's A and B codes
+      // are the translated oriented reads and the resident contig codes)
+      if (!rc && out->cigar_slot && mhsw::driver_cigar(d)) {
+        ps.a_code = mhsw::driver_a_codes(d);
+        rc = mhsw::cigar_resident(d, ps);
+      }
     }
     if (n_aligned) *n_aligned = m;
   }
@@ -373,6 +379,7 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
     down(out->identity, o_id, sizeof(int32_t) * n);
     down(out->orient, o_or, (size_t)n);
     down(out->perfect, o_pf, (size_t)n);
+    if (out->cigar_slot && mhsw::driver_cigar(d)) down(out->cigar_slot, slot, sizeof(int32_t) * n);
     if (!e) e = cudaStreamSynchronize(st);
   }
   for (void *p : allocs) cudaFreeAsync(p, st);

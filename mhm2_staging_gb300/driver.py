@@ -141,7 +141,7 @@ class CandidatesT(C.Structure):
 
 class AlnsT(C.Structure):
     _fields_ = [("rstart", _P), ("rstop", _P), ("cstart", _P), ("cstop", _P), ("score1", _P), ("score2", _P),
-                ("identity", _P), ("orient", _P), ("perfect", _P)]
+                ("identity", _P), ("orient", _P), ("perfect", _P), ("cigar_slot", _P)]
 
 
 SIGNATURES: dict[str, tuple] = {

@@ -73,9 +73,10 @@ class ResidentContigs:
         self.close()
 
 
-def klign_align(drv: "D.GPUDriver", rc: ResidentContigs, cand: Candidates) -> dict:
+def klign_align(drv: "D.GPUDriver", rc: ResidentContigs, cand: Candidates, cigars: bool = False) -> dict:
     """Aln fields per candidate (rstart, rstop, cstart, cstop, score1, score2, identity,
-    orient as b'+'/b'-' codes, perfect) and n_aligned, as mhsw_klign_align computes them."""
+    orient as b'+'/b'-' codes, perfect) and n_aligned, as mhsw_klign_align computes them;
+    with cigars (the driver in CIGAR mode) also klign's SAM CIGAR string and mismatches."""
     n = cand.n
     arrs = {k: np.zeros(n, dtype=np.int32) for k in ("rstart", "rstop", "cstart", "cstop", "score1", "score2",
                                                      "identity")}
@@ -85,11 +86,20 @@ def klign_align(drv: "D.GPUDriver", rc: ResidentContigs, cand: Candidates) -> di
                                                            (cand.cid, np.int32), (cand.pos_in_ctg, np.int32),
                                                            (cand.pos_in_read, np.int32), (cand.strand, np.uint8))]
     ct = D.CandidatesT(cand.read_seq.ctypes.data, *(k.ctypes.data for k in keep), n, cand.kmer_len)
+    slot = np.full(n, -1, dtype=np.int32)
     at = D.AlnsT(*(arrs[k].ctypes.data for k in ("rstart", "rstop", "cstart", "cstop", "score1", "score2",
-                                                  "identity", "orient", "perfect")))
+                                                  "identity", "orient", "perfect")), slot.ctypes.data if cigars else None)
     m = C.c_int64(0)
     drv._ck(drv._lib.mhsw_klign_align(drv._h, rc.handle, C.byref(ct), C.byref(at), C.byref(m)), "klign_align")
     arrs["n_aligned"] = int(m.value)
+    if cigars:
+        # klign's SAM fields: "<overlap>=" and 0 mismatches for a perfect match (src/klign.cpp:229),
+        # SSW's cigar_string and mismatches for the aligned candidates
+        cg = drv.last_cigar(arrs["n_aligned"])
+        arrs["cigar"] = [cg.string(int(j)) if j >= 0 else f"{arrs['rstop'][i] - arrs['rstart'][i]}="
+                         for i, j in enumerate(slot)]
+        arrs["mismatches"] = np.where(slot >= 0, cg.mismatches[np.maximum(slot, 0)] if len(cg.mismatches) else 0,
+                                      0).astype(np.int32)
     return arrs
 
 

@@ -35,9 +35,11 @@ for _c in b"URYKMSWBDHV":
 def klign_align(contig_seq: np.ndarray, contig_off: np.ndarray, contig_len: np.ndarray, read_seq: np.ndarray,
                 read_off: np.ndarray, read_len: np.ndarray, cid: np.ndarray, pos_in_ctg: np.ndarray,
                 pos_in_read: np.ndarray, strand: np.ndarray, kmer_len: int, scoring=(1, 3, 5, 2, 2),
-                score2: bool = False, threads: int | None = None) -> dict:
+                score2: bool = False, threads: int | None = None, cigars: bool = False) -> dict:
     """Per-candidate Aln fields: rstart, rstop, cstart, cstop, score1, score2, identity,
-    orient ('+'/'-' as bytes), perfect (0/1); plus n_aligned."""
+    orient ('+'/'-' as bytes), perfect (0/1); plus n_aligned.  cigars: also klign's SAM
+    CIGAR string and mismatches -- "<overlap>=" and 0 for a perfect match (klign.cpp:229),
+    SSW's cigar_string and mismatches (report_cigar) for the others (:271, :268)."""
     from mhm2_staging_gb300.driver import Pairs
 
     n = int(read_len.shape[0])
@@ -76,9 +78,16 @@ def klign_align(contig_seq: np.ndarray, contig_off: np.ndarray, contig_len: np.n
     ce = cstart + ov
     sc = ov * match
     s2 = np.zeros(n, dtype=np.int64)
+    cig = [f"{int(o)}=" for o in ov]
+    mism = np.zeros(n, dtype=np.int32)
     if len(idx):
         pairs = Pairs(ori, read_off[idx].astype(np.int64), read_len[idx].astype(np.int32), contig_seq,
                       coff[idx].astype(np.int64), ov[idx].astype(np.int32))
+        if cigars:
+            cout, cops, cn = oracle.cigar_batch(pairs, scoring, threads, ops_cap=2048)
+            for t, i in enumerate(idx):
+                cig[i] = oracle.cigar_string(cops[t], max(int(cn[t]), 0))
+                mism[i] = cout[t, 5]
         res = oracle.align_batch(pairs, scoring, threads, score2=score2).astype(np.int64)
         sc[idx] = res[:, 0]
         rs[idx] = res[:, 1]
@@ -93,4 +102,5 @@ def klign_align(contig_seq: np.ndarray, contig_off: np.ndarray, contig_len: np.n
     return {"rstart": rs2.astype(np.int32), "rstop": re2.astype(np.int32), "cstart": cs.astype(np.int32),
             "cstop": ce.astype(np.int32), "score1": sc.astype(np.int32), "score2": s2.astype(np.int32),
             "identity": ident.astype(np.int32), "orient": np.where(minus, ord("-"), ord("+")).astype(np.uint8),
-            "perfect": perfect.astype(np.uint8), "n_aligned": int(len(idx))}
+            "perfect": perfect.astype(np.uint8), "n_aligned": int(len(idx)),
+            **({"cigar": cig, "mismatches": mism} if cigars else {})}

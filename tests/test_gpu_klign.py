@@ -87,3 +87,21 @@ def test_klign_caller_rejects_bad_candidates(contigs, resident):
     got = klign_align(d, resident, cand)
     assert not _diff(got, _want(contigs, cand, (1, 3, 5, 2, 2), False))
     assert klign_align(d, resident, cand.slice(0, 0))["n_aligned"] == 0
+
+
+def test_klign_caller_sam_cigars(contigs, resident):
+    """CIGAR mode: klign's SAM CIGAR per candidate -- "<overlap>=" for the perfect matches,
+    SSW's cigar_string for the aligned ones -- and mismatches, with the post-assembly
+    scoring 2/4/4/2/1 klign uses when it asks for CIGARs."""
+    sc = (2, 4, 4, 2, 1)
+    cand = generate_candidates(contigs, 20000, seed=33)
+    d = _driver(sc)
+    d.set_cigar(True)
+    got = klign_align(d, resident, cand, cigars=True)
+    want = klign_caller.klign_align(contigs.seq, contigs.off, contigs.len, cand.read_seq, cand.read_off,
+                                    cand.read_len, cand.cid, cand.pos_in_ctg, cand.pos_in_read, cand.strand,
+                                    cand.kmer_len, sc, False, cigars=True)
+    assert not _diff(got, want)
+    bad = [i for i in range(cand.n) if got["cigar"][i] != want["cigar"][i]]
+    assert not bad, (len(bad), got["cigar"][bad[0]], want["cigar"][bad[0]])
+    assert np.array_equal(got["mismatches"], want["mismatches"])
