@@ -283,7 +283,18 @@ __global__ void __launch_bounds__(256) k_rev_scatter(ResultSet rs, Scoring sc, c
 // PAD code, which scores -128: cells left of column 0 then stay exactly at the boundary
 // values and cells right of the last column stay below the score, so the band needs no
 // per-cell bound checks.
-template <int W, int NC>
+// BI: the table bytes already hold s + gO (every score >= -gO; PAD scores -gO), and
+// Hdiag + byte is a multiply-add by a runtime 1 (bias then carries that 1), which issues
+// on the FMA pipe instead of the integer ALU pipe the band saturates.  A PAD score of -gO
+// keeps the cells left of column 0 at exactly 0 (their diagonal, above and left values
+// are 0) and every cell right of the last column at most a real cell's H - gO.
+template <bool BI>
+__device__ __forceinline__ int band_q(int hd, uint32_t byte, int bias) {
+  if constexpr (BI) return (int)mad_u32((uint32_t)hd, (uint32_t)bias, byte);
+  else return hd + (int)byte + bias;
+}
+
+template <int W, int NC, bool BI>
 __device__ __forceinline__ int band_row(const int (&cb)[NC], int u, uint32_t rp0, uint32_t rp1, int bias, int ngo,
                                         int nge, int (&H)[W + 1], int (&E)[W + 1]) {
   constexpr int NEG = -(1 << 28);
@@ -291,7 +302,7 @@ __device__ __forceinline__ int band_row(const int (&cb)[NC], int u, uint32_t rp0
   int rm = 0;
 #pragma unroll
   for (int d = 0; d < W; d++) {
-    const int q = H[d] + (int)__byte_perm(rp0, rp1, (uint32_t)cb[u + d]) + bias;  // Hdiag + s + gO
+    const int q = band_q<BI>(H[d], __byte_perm(rp0, rp1, (uint32_t)cb[u + d]), bias);  // Hdiag + s + gO
     const int e = __viaddmax_s32(E[d + 1], nge, H[d + 1]);
     const int h = __viaddmax_s32_relu(__vimax3_s32(q, e, F), ngo, 0);
     F = __viaddmax_s32(F, nge, h);
@@ -302,11 +313,52 @@ __device__ __forceinline__ int band_row(const int (&cb)[NC], int u, uint32_t rp0
   return rm;
 }
 
+// Two band rows at once: row A (window offset u) and the row below it, B (offset u + 1),
+// two cells behind.  B's cell d reads A's cells d (diagonal) and d + 1 (above), written
+// at the two steps before, and overwrites A's cell d, which nothing needs any more; A's
+// cell s reads only cells >= s of the row above.  The two rows' dependency chains (F
+// along each row) are independent within a step, so they interleave; the arithmetic is
+// band_row's, cell for cell.  Returns the larger of the two rows' maxima.
+template <int W, int NC, bool BI>
+__device__ __forceinline__ int band_row2(const int (&cb)[NC], int u, uint32_t ra0, uint32_t ra1, uint32_t rb0,
+                                         uint32_t rb1, int bias, int ngo, int nge, int (&H)[W + 1], int (&E)[W + 1]) {
+  constexpr int NEG = -(1 << 28);
+  int FA = NEG, FB = NEG;
+  int rm = 0;
+#pragma unroll
+  for (int s = 0; s < W + 2; s++) {
+    int ha = 0, hb = 0;
+    if (s < W) {
+      const int q = band_q<BI>(H[s], __byte_perm(ra0, ra1, (uint32_t)cb[u + s]), bias);
+      const int e = __viaddmax_s32(E[s + 1], nge, H[s + 1]);
+      ha = __viaddmax_s32_relu(__vimax3_s32(q, e, FA), ngo, 0);
+      FA = __viaddmax_s32(FA, nge, ha);
+      E[s] = e;
+      H[s] = ha;
+    }
+    if (s >= 2) {
+      const int d = s - 2;
+      const int q = band_q<BI>(H[d], __byte_perm(rb0, rb1, (uint32_t)cb[u + 1 + d]), bias);
+      const int e = __viaddmax_s32(E[d + 1], nge, H[d + 1]);
+      hb = __viaddmax_s32_relu(__vimax3_s32(q, e, FB), ngo, 0);
+      FB = __viaddmax_s32(FB, nge, hb);
+      E[d] = e;
+      H[d] = hb;
+    }
+    rm = __vimax3_s32(rm, ha, hb);
+  }
+  return rm;
+}
+
 // Pass 3 (one launch per class C): the banded search over the class's segment.  Rows go
 // in blocks of U; the band's codes live in a register window of W + U columns that
 // slides by U columns per block (one load per new column), and the row's scores come from
-// a per-block table indexed by the A code.
-template <int WB, int C>
+// a per-block table indexed by the A code.  A row's maximum exceeds the largest maximum
+// of the rows before it by at most match (H <= Hdiag + match; E and F only lose), so
+// while that running maximum is below S - 2 * match neither of the next two rows can
+// reach S: those go two at a time (band_row2) with no search for the first cell; the
+// rows that may reach S go one at a time.
+template <int WB, int C, bool BI>
 __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl) {
   constexpr int NEG = -(1 << 28);
   constexpr int G = WB / 2 - 1;
@@ -314,21 +366,24 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
   constexpr int U = W <= 15 ? 8 : (W <= 31 ? 4 : 2);
   constexpr int NC = W + U;
   static_assert(G == band_half(C), "band class and width disagree");
-  __shared__ uint32_t rptab[2 * 8];  // per A code 0..4: s(a, c) + 128 as bytes c = 0..3 | c = 4, PAD
+  // per A code 0..4: s(a, c) + off as bytes c = 0..3 | c = 4, PAD; off = gO (BI) or 128
+  __shared__ uint32_t rptab[2 * 8];
+  const int toff = BI ? sc.gap_open : 128;
   if (threadIdx.x < 5) {
     const int a = threadIdx.x;
     uint32_t r0 = 0, r1 = 0;
     for (int c = 0; c < 5; c++) {
-      const uint32_t v = (uint32_t)(sub_score(a, c, sc, 128) + 128) & 0xffu;
+      const uint32_t v = (uint32_t)(sub_score(a, c, sc, 128) + toff) & 0xffu;
       if (c < 4) r0 |= v << (8 * c);
-      else r1 = v;  // byte 1 (PAD) and above stay 0: score -128
+      else r1 = v;  // byte 1 (PAD) and above stay 0: score -off
     }
     rptab[2 * a] = r0;
     rptab[2 * a + 1] = r1;
   }
   __syncthreads();
   const int mt = sc.match;
-  const int bias = sc.gap_open - 128, ngo = -sc.gap_open, nge = -sc.gap_extend;
+  // BI: bias is a 1 the compiler cannot fold (gap_open is positive and below 2^30)
+  const int bias = BI ? (sc.gap_open >> 30) + 1 : sc.gap_open - 128, ngo = -sc.gap_open, nge = -sc.gap_extend;
   int64_t off = 0;
 #pragma unroll
   for (int c = 0; c < C; c++) off += wl.band_counts[c];
@@ -357,27 +412,43 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
 #pragma unroll
     for (int k = 0; k < NC; k++) cb[k] = code_at(k - G);
     int i = 0;  // first row of the current block; the window covers columns i - G + [0, NC)
+    int rrun = 0;  // largest row maximum so far
     for (;;) {
       if (band_gap_bound(t, N2, S, sc) > G) {
         escalate = true;
         break;
       }
       while (i < t && !found) {
+        static_assert(U % 2 == 0, "rows go in pairs within a block");
 #pragma unroll
-        for (int u = 0; u < U; u++) {
+        for (int u = 0; u < U; u += 2) {
           const int row = i + u;
           if (!found && row < t) {
-            const int ca = a[-row];
-            const int rm = band_row<W, NC>(cb, u, rptab[2 * ca], rptab[2 * ca + 1], bias, ngo, nge, H, E);
-            if (rm >= S) {
-              // first cell of this row that reaches the score
+            if (row + 1 < t && rrun < S - 2 * mt) {
+              const int ca = a[-row], cc = a[-(row + 1)];
+              const int rm = band_row2<W, NC, BI>(cb, u, rptab[2 * ca], rptab[2 * ca + 1], rptab[2 * cc],
+                                              rptab[2 * cc + 1], bias, ngo, nge, H, E);
+              rrun = max(rrun, rm);
+            } else {
 #pragma unroll
-              for (int d = 0; d < W; d++) {
-                const int j = row - G + d;
-                if (!found && j >= 0 && j < N2 && H[d] >= S) {
-                  found = true;
-                  fi = row;
-                  fj = j;
+              for (int v = 0; v < 2; v++) {
+                const int r = row + v;
+                if (!found && r < t) {
+                  const int ca = a[-r];
+                  const int rm = band_row<W, NC, BI>(cb, u + v, rptab[2 * ca], rptab[2 * ca + 1], bias, ngo, nge, H, E);
+                  rrun = max(rrun, rm);
+                  if (rm >= S) {
+                    // first cell of this row that reaches the score
+#pragma unroll
+                    for (int d = 0; d < W; d++) {
+                      const int j = r - G + d;
+                      if (!found && j >= 0 && j < N2 && H[d] >= S) {
+                        found = true;
+                        fi = r;
+                        fj = j;
+                      }
+                    }
+                  }
                 }
               }
             }
@@ -783,13 +854,26 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
       if (e != cudaSuccess) return e;
     }
     for (int c = 0; c < kBandClasses; c++) cs[c] = fan ? fk->side[c] : st;
-    k_rev_band<64, 6><<<gridb, 128, 0, cs[6]>>>(ps, rs, sc, wl);
-    k_rev_band<48, 5><<<gridb, 128, 0, cs[5]>>>(ps, rs, sc, wl);
-    k_rev_band<32, 4><<<gridb, 128, 0, cs[4]>>>(ps, rs, sc, wl);
-    k_rev_band<24, 3><<<gridb, 128, 0, cs[3]>>>(ps, rs, sc, wl);
-    k_rev_band<16, 2><<<gridb, 128, 0, cs[2]>>>(ps, rs, sc, wl);
-    k_rev_band<12, 1><<<gridb, 128, 0, cs[1]>>>(ps, rs, sc, wl);
-    k_rev_band<8, 0><<<gridb, 128, 0, cs[0]>>>(ps, rs, sc, wl);
+    // scores s + gO as bytes when no penalty exceeds the gap-open penalty (klign's scorings)
+    const bool bi = sc.gap_open > 0 && sc.mismatch <= sc.gap_open && sc.ambiguity <= sc.gap_open &&
+                    sc.match + sc.gap_open <= 255;
+    if (bi) {
+      k_rev_band<64, 6, true><<<gridb, 128, 0, cs[6]>>>(ps, rs, sc, wl);
+      k_rev_band<48, 5, true><<<gridb, 128, 0, cs[5]>>>(ps, rs, sc, wl);
+      k_rev_band<32, 4, true><<<gridb, 128, 0, cs[4]>>>(ps, rs, sc, wl);
+      k_rev_band<24, 3, true><<<gridb, 128, 0, cs[3]>>>(ps, rs, sc, wl);
+      k_rev_band<16, 2, true><<<gridb, 128, 0, cs[2]>>>(ps, rs, sc, wl);
+      k_rev_band<12, 1, true><<<gridb, 128, 0, cs[1]>>>(ps, rs, sc, wl);
+      k_rev_band<8, 0, true><<<gridb, 128, 0, cs[0]>>>(ps, rs, sc, wl);
+    } else {
+      k_rev_band<64, 6, false><<<gridb, 128, 0, cs[6]>>>(ps, rs, sc, wl);
+      k_rev_band<48, 5, false><<<gridb, 128, 0, cs[5]>>>(ps, rs, sc, wl);
+      k_rev_band<32, 4, false><<<gridb, 128, 0, cs[4]>>>(ps, rs, sc, wl);
+      k_rev_band<24, 3, false><<<gridb, 128, 0, cs[3]>>>(ps, rs, sc, wl);
+      k_rev_band<16, 2, false><<<gridb, 128, 0, cs[2]>>>(ps, rs, sc, wl);
+      k_rev_band<12, 1, false><<<gridb, 128, 0, cs[1]>>>(ps, rs, sc, wl);
+      k_rev_band<8, 0, false><<<gridb, 128, 0, cs[0]>>>(ps, rs, sc, wl);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (fan) {

@@ -57,6 +57,22 @@ def test_dropin_protocol_klign(gpu):
     assert np.array_equal(r1.query_end32, r.query_end32) and np.array_equal(r1.ref_end32, r.ref_end32)
 
 
+@pytest.mark.parametrize("sc", [(1, 6, 4, 1, 3), (1, 2, 3, 1, 4)])
+@pytest.mark.parametrize("cfg", [1, 2])
+def test_penalties_above_gap_open(built, sc, cfg):
+    """A mismatch or ambiguity penalty above the gap-open penalty: the forward pass takes
+    the generic int32 engine and the begin pass the band kernels' offset-128 score table."""
+    m, x, go, ge, amb = sc
+    d = GPUDriver()
+    d.init(0, 1, m, -x, -go, -ge, 0)
+    d.set_ambiguity(-amb)
+    pairs = workloads.generate(cfg, n=6000)
+    want = oracle.align_batch(pairs, sc)
+    for form in (FORM_PLAIN, FORM_BATCHED):
+        got = d.align_pairs(pairs, form=form)
+        assert not _diff(got, want, pairs)
+
+
 def test_forced_int32_rerun(built):
     d = GPUDriver()
     d.init(0, 1, 1, -3, -5, -2, 300)
