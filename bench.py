@@ -394,7 +394,7 @@ def main() -> None:
     ap.add_argument("--ref-pairs", type=int, default=20000, help="pairs per step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--no-paths", action="store_true", help="skip the per-workload path measurements")
     ap.add_argument("--cigar", action="store_true",
                     help="CIGAR mode in the timed regions (SSW's report_cigar output as well; e2e copies it back)")
