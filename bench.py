@@ -110,6 +110,41 @@ def cpu_baseline(pairs, budget_s: float = 12.0) -> dict:
             "alignments_per_s": n / dt}
 
 
+def _adept_gpu(args) -> dict | None:
+    """ADEPT, the reference's own CUDA kernels for this path (compiled for sm_103a from the
+    reference sources into oracle/_ref), on the main arm's workload with inputs resident:
+    the same-GPU comparator.  None when the cubin or a GPU is missing."""
+    import torch
+    from oracle import adept
+
+    if not (adept.available() and torch.cuda.is_available()):
+        return None
+    from mhm2_staging_gb300 import workloads
+    from oracle import oracle
+
+    n = args.pairs or workloads.CONFIG_PAIRS[args.config]
+    pairs = workloads.generate(args.config, n=n)
+    ad = adept.Adept(0)
+    batch = ad.upload(pairs)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    fwd, rev, tot = [], [], []
+    for s in range(args.warmup + args.steps):
+        ad.run(batch, SCORING, 0, ev)
+        if s >= args.warmup:
+            fwd.append(ev[0].elapsed_time(ev[1]))
+            rev.append(ev[2].elapsed_time(ev[3]))
+            tot.append(ev[0].elapsed_time(ev[3]))
+    k = min(n, 20000)
+    want = oracle.align_batch(pairs.slice(0, k), SCORING, None)[:, 0]
+    agree = float((ad.scores(batch)[:k] == want).mean())
+    ms = statistics.mean(tot)
+    return {"value": pairs.cells() / (ms * 1e-3) / 1e9, "unit": "GCUPS", "ms_per_step": ms,
+            "fwd_ms": statistics.mean(fwd), "rev_ms": statistics.mean(rev), "pairs": n,
+            "kernels": "ADEPT sequence_dna_kernel + sequence_dna_reverse (src/adept-sw/kernel.cpp) compiled "
+                       "for sm_103a, launched with the reference driver's shapes, inputs resident",
+            "score_agreement_with_oracle": agree, "agreement_sample": k}
+
+
 def run_reference(args) -> None:
     ws, rank, _ = _dist()
     if rank != 0:
@@ -144,6 +179,9 @@ def run_reference(args) -> None:
                                    f"only; this is the C restatement of its result contract)"},
         "e2e": {"value": gcups, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    ad = _adept_gpu(args)
+    if ad is not None:
+        line["adept_gpu"] = ad
     print(json.dumps(line), flush=True)
 
 

@@ -14,6 +14,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import platform
+import shutil
 import subprocess
 from pathlib import Path
 
@@ -30,12 +31,15 @@ _REF = None
 
 
 def build(with_reference: bool | None = None) -> None:
-    """Builds liboracle.so, and libssw_ref.so when the reference checkout is present."""
+    """Builds liboracle.so; where the reference checkout is present, also libssw_ref.so
+    (x86_64) and the ADEPT comparator cubin (any host with nvcc)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "_build/liboracle.so"], check=True)
-    if with_reference is None:
-        with_reference = (REFERENCE_ROOT / "src" / "ssw" / "ssw.cpp").exists() and platform.machine() == "x86_64"
-    if with_reference:
+    if with_reference is False:
+        return
+    if (REFERENCE_ROOT / "src" / "ssw" / "ssw.cpp").exists() and platform.machine() == "x86_64":
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_ROOT}"], check=True)
+    if (REFERENCE_ROOT / "src" / "adept-sw" / "kernel.cpp").exists() and shutil.which("nvcc"):
+        subprocess.run(["make", "-s", "-C", str(HERE), "adept", f"REF={REFERENCE_ROOT}"], check=True)
 
 
 def _bind(lib: C.CDLL, name: str) -> None:
