@@ -318,7 +318,29 @@ def run_paths(drv, dev, torch, stream) -> dict:
     drv.set_cigar(False)
     out["klign_caller_200k_candidates"] = _klign_caller_path(drv)
     out["protein_100k_pairs_100_500aa"] = _protein_path()
+    out["uneven_1M_pairs_in_20k_pair_calls_host"] = _block_calls_path(drv)
     return out
+
+
+def _block_calls_path(drv, n: int = 1_000_000, per_call: int = 20_000) -> dict:
+    """klign's call size (KLIGN_GPU_BLOCK_SIZE, 20,000 pairs): the uneven workload's first
+    1M pairs in 20,000-pair synchronous calls through the C ABI from host (pageable) arrays,
+    as klign's strings are; copies in, both passes and results out inside each call.  Plain
+    and batched form."""
+    from mhm2_staging_gb300 import FORM_BATCHED, FORM_PLAIN, workloads
+
+    pp = workloads.generate(2, n=n)
+    blocks = [pp.slice(i, i + per_call) for i in range(0, pp.n, per_call)]
+    res = {"pairs": pp.n, "pairs_per_call": per_call, "calls": len(blocks), "cells": float(pp.cells())}
+    for name, form in (("plain", FORM_PLAIN), ("batched", FORM_BATCHED)):
+        for b in blocks[:2]:
+            drv.align_pairs(b, form=form, hints=True)
+        t0 = time.perf_counter()
+        for b in blocks:
+            drv.align_pairs(b, form=form, hints=True)
+        dt = time.perf_counter() - t0
+        res[name] = {"alignments_per_s": pp.n / dt, "gcups": pp.cells() / dt / 1e9, "ms_per_call": 1e3 * dt / len(blocks)}
+    return res
 
 
 def _protein_pairs(n: int, seed: int = 8):
