@@ -89,25 +89,31 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+CPU_PORT = ("the oracle's result contract vectorised across pairs (oracle/sw_lanes.cpp: 8 pairs per 128-bit "
+            "vector, portable GCC vectors; bit-exact with the scalar restatement; on x86_64 it matches the reference "
+            "SSE2 SSW's speed on the same pairs and threads)")
+
+
 def cpu_baseline(pairs, budget_s: float = 12.0) -> dict:
-    """The oracle port timed on the host cores on a bounded leading sample of the batch."""
+    """The oracle port (vectorised across pairs) timed on the host cores on a bounded
+    leading sample of the batch."""
     from oracle import oracle
 
     threads = os.cpu_count() or 1
-    n_probe = min(pairs.n, 2000)
+    n_probe = min(pairs.n, 20000)
     probe = pairs.slice(0, n_probe)
     t0 = time.perf_counter()
-    oracle.align_batch(probe, SCORING, threads)
+    oracle.align_batch_lanes(probe, SCORING, threads)
     dt = max(time.perf_counter() - t0, 1e-3)
     n = int(min(pairs.n, max(n_probe, n_probe * budget_s / dt)))
     sample = pairs.slice(0, n)
     t0 = time.perf_counter()
-    oracle.align_batch(sample, SCORING, threads)
+    oracle.align_batch_lanes(sample, SCORING, threads)
     dt = time.perf_counter() - t0
     cells = sample.cells()
     return {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
             "sample": f"first {n} pairs of the same workload ({cells:.3g} forward cells, {dt:.1f} s)",
-            "alignments_per_s": n / dt}
+            "implementation": CPU_PORT, "alignments_per_s": n / dt}
 
 
 def _adept_gpu(args) -> dict | None:
@@ -160,7 +166,7 @@ def run_reference(args) -> None:
     for s in range(args.warmup + args.steps):
         sub = pairs.slice(s * per_step, (s + 1) * per_step)
         t0 = time.perf_counter()
-        oracle.align_batch(sub, SCORING, threads)
+        oracle.align_batch_lanes(sub, SCORING, threads)
         dt = time.perf_counter() - t0
         if s >= args.warmup:
             times.append(dt)
@@ -175,8 +181,9 @@ def run_reference(args) -> None:
                    "cache": "inputs larger than L2 (CPU run)"},
         "alignments_per_s": per_step * args.steps / tot,
         "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": threads, "kind": "port",
-                         "sample": f"{per_step} pairs per step of the same workload (reference SSW is x86/PPC "
-                                   f"only; this is the C restatement of its result contract)"},
+                         "sample": f"{per_step} pairs per step of the same workload (the reference SSW has only "
+                                   f"SSE2 and AltiVec code and its sources do not ship to this host)",
+                         "implementation": CPU_PORT},
         "e2e": {"value": gcups, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     ad = _adept_gpu(args)
@@ -451,7 +458,7 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--pairs", type=int, default=None, help="override pairs per GPU (smaller runs)")
-    ap.add_argument("--ref-pairs", type=int, default=20000, help="pairs per step of the reference arm")
+    ap.add_argument("--ref-pairs", type=int, default=200000, help="pairs per step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)

@@ -64,6 +64,7 @@ def oracle_lib() -> C.CDLL:
         lib = C.CDLL(str(ORACLE_SO))
         _bind(lib, "sw_oracle_align_batch")
         _bind(lib, "sw_oracle_align_batch7")
+        _bind(lib, "sw_oracle_align_batch_lanes")
         _bind_cigar(lib, "sw_oracle_cigar_batch")
         lib.sw_oracle_protein_batch.restype = C.c_int
         lib.sw_oracle_protein_batch.argtypes = [C.c_char_p, _P, _P, C.c_char_p, _P, _P, C.c_int64, _P, _P, C.c_int,
@@ -118,6 +119,12 @@ def align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, scor
     if score2:
         return _run(oracle_lib(), "sw_oracle_align_batch7", pairs, scoring, threads or (os.cpu_count() or 1), 7)
     return _run(oracle_lib(), "sw_oracle_align_batch", pairs, scoring, threads or (os.cpu_count() or 1))
+
+
+def align_batch_lanes(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None) -> np.ndarray:
+    """align_batch's results (n x 5) from the across-pairs vectorised restatement
+    (sw_lanes.cpp): eight pairs per 128-bit vector, the CPU baseline's implementation."""
+    return _run(oracle_lib(), "sw_oracle_align_batch_lanes", pairs, scoring, threads or (os.cpu_count() or 1))
 
 
 def ref_align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, score2: bool = False) -> np.ndarray:

@@ -71,6 +71,54 @@ def test_zero_score_and_empty_conventions():
     assert out.tolist() == [[0, -1, -1, 0, 0]] * 4
 
 
+def _tie_heavy_pairs(seed, n=400):
+    rng = random.Random(seed)
+    alphabets = ["ACGT", "AC", "A", "ACGTN", "acgtU", "ACGTNX"]
+    a, b = [], []
+    for _ in range(n):
+        al = rng.choice(alphabets)
+        la, lb = rng.randint(1, 60), rng.randint(1, 90)
+        x = "".join(rng.choice(al) for _ in range(la))
+        if rng.random() < 0.5:
+            y = "".join(rng.choice(al) for _ in range(lb))
+        else:
+            k = rng.randint(0, lb)
+            y = "".join(rng.choice(al) for _ in range(k)) + x + "".join(rng.choice(al) for _ in range(rng.randint(0, 20)))
+        a.append(x)
+        b.append(y)
+    return a, b
+
+
+@pytest.mark.parametrize("sc", [(1, 3, 5, 2, 2), (2, 4, 4, 2, 1), (1, 2, 3, 1, 4), (2, 2, 3, 1, 2), (1, 1, 1, 1, 1),
+                                (1, 3, 5, 2, 0)])
+def test_vectorised_restatement_equals_scalar(sc):
+    """sw_lanes.cpp (eight pairs per vector, the CPU baseline) against the scalar
+    restatement: tie-heavy pairs, empty and all-N sequences, the generated workloads, and
+    the scalar fallbacks (scores that could leave int16; ambiguity 0)."""
+    from mhm2_staging_gb300 import workloads
+
+    a, b = _tie_heavy_pairs(7, 600)
+    a += ["", "ACGT", "NNNN", "A" * 300, "ACGT" * 75]
+    b += ["ACGT", "", "NNNN", "A" * 310, "ACGT" * 80]
+    batches = [Pairs.from_lists(a, b)] + [workloads.generate(cfg, n=n) for cfg, n in ((0, 600), (1, 900), (2, 900))]
+    for p in batches:
+        got = oracle.align_batch_lanes(p, sc, 4)
+        want = oracle.align_batch(p, sc, 4)
+        bad = np.nonzero((got != want).any(axis=1))[0]
+        assert len(bad) == 0, (sc, bad[:3].tolist(), got[bad[:3]].tolist(), want[bad[:3]].tolist())
+
+
+def test_vectorised_restatement_near_the_int16_range():
+    """match 90 on 300-base pairs (scores up to 27000) stays in the vector lanes; match 100
+    (30000) goes to the scalar restatement; both equal it."""
+    rng = random.Random(3)
+    a = ["".join(rng.choice("ACGT") for _ in range(300)) for _ in range(20)]
+    b = [x[: rng.randint(250, 300)] if k % 2 else x for k, x in enumerate(a)]
+    p = Pairs.from_lists(a, b)
+    for sc in ((90, 3, 5, 2, 2), (100, 3, 5, 2, 2)):
+        assert np.array_equal(oracle.align_batch_lanes(p, sc, 2), oracle.align_batch(p, sc, 2)), sc
+
+
 @pytest.mark.skipif(not oracle.reference_available(), reason="reference SSW not built (needs the reference checkout)")
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_random_pairs_vs_live_reference(seed):
