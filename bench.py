@@ -90,8 +90,8 @@ class ClockSampler:
 
 
 CPU_PORT = ("the oracle's result contract vectorised across pairs (oracle/sw_lanes.cpp: 8 pairs per 128-bit "
-            "vector, portable GCC vectors; bit-exact with the scalar restatement; on x86_64 it matches the reference "
-            "SSE2 SSW's speed on the same pairs and threads)")
+            "vector, 4 vectors interleaved on aarch64, portable GCC vectors; bit-exact with the scalar restatement; "
+            "on x86_64 it matches the reference SSE2 SSW's speed on the same pairs and threads)")
 
 
 def cpu_baseline(pairs, budget_s: float = 12.0) -> dict:
