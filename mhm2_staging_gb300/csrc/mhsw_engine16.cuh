@@ -29,8 +29,8 @@
 //     words (every load is a full 128-bit vector, conflict-free across the groups of a
 //     warp).  The high words loaded at step t serve the high half at step t+1 (the step
 //     loop is unrolled by two so the two word sets alternate registers).
-//  4. B codes are read from global memory (prefetched a step ahead) instead of being
-//     staged in shared memory, so a group's shared memory is its profile table only.
+//  4. B codes are read from global memory (each loaded two steps before its use) instead
+//     of being staged in shared memory, so a group's shared memory is its profile table only.
 //
 // Score2 mode (S2) also produces what SSW's second-best score is computed from
 // (ssw_core.cpp:489, :513-536): each A row's maximum of H, over B extended to P columns
@@ -181,7 +181,7 @@ struct Step16 {
 };
 
 // Forward sweep of one pair with the keyed engine.  B is read directly from its code
-// array in global memory (one byte per lane per step, prefetched a step ahead); the
+// array in global memory (one byte per lane per step, loaded two steps ahead); the
 // shared memory of the group holds only the profile table.  A must be a forward view.
 template <int K, int G, bool MULTI, bool S2 = false>
 __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &sc, const GroupSmem &gs, int lane,
@@ -260,7 +260,8 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
       const uint32_t hi = (unsigned)(jl - 1) < (unsigned)NP ? 0u : 0xC0000000u;
       return lo | hi;
     };
-    int cnext = code_at(j0);
+    // codes of the even and odd steps, each loaded two steps before its use
+    int ceven = code_at(j0), codd = code_at(j0 + 1);
 
     auto top = [&](int t, uint32_t zs) -> uint32_t {
       uint32_t z = zs & zmask;
@@ -276,17 +277,15 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
     int t = 0;
     for (; t + 1 < T_end; t += 2) {
       // even step: hi words into HA; the high half uses HB (previous column)
-      int c = cnext;
-      int jn = t + 1 + j0;
-      cnext = code_at(jn);
+      int c = ceven;
+      ceven = code_at(t + 2 + j0);
       ST::load(tab, c, lane, Wlo, HA);
       uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
       ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale, Rm, vmask_at(t));
       out_bnd(t);
       // odd step: hi words into HB; the high half uses HA
-      c = cnext;
-      jn = t + 2 + j0;
-      cnext = code_at(jn);
+      c = codd;
+      codd = code_at(t + 3 + j0);
       ST::load(tab, c, lane, Wlo, HB);
       z = top(t + 1, __shfl_up_sync(gmask, Zout, 1, G));
       ST::run(t + 1, z, Wlo, HA, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale, Rm,
@@ -294,7 +293,7 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
       out_bnd(t + 1);
     }
     if (t < T_end) {
-      ST::load(tab, cnext, lane, Wlo, HA);
+      ST::load(tab, ceven, lane, Wlo, HA);
       const uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
       ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale, Rm, vmask_at(t));
       out_bnd(t);
