@@ -541,17 +541,21 @@ __global__ void k_translate(const char *__restrict__ src, uint8_t *__restrict__ 
   for (int64_t i = done + tid; i < nbytes; i += stride) dst[i] = tab[(unsigned char)src[i]];
 }
 
-// Wavefront begin search on the reversed box for the pairs listed in wl.wide.
-template <int K, int G>
-__global__ void __launch_bounds__(256) k_rev_wave(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl, V32::Pay *scratch,
-                                                  int scratch_stride, int pad, int bcap) {
+// Wavefront begin search on the reversed box for the pairs listed in wl.wide whose score
+// lies in [s_lo, s_hi].  No cell of the reversed box exceeds the score, so int16 values
+// (V16) are exact for scores up to kWaveScore16; the int32 instantiation takes the rest.
+constexpr int kWaveScore16 = 16000;
+template <class VT, int K, int G>
+__global__ void __launch_bounds__(256) k_rev_wave(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl,
+                                                  typename VT::Pay *scratch, int scratch_stride, int pad, int bcap,
+                                                  int s_lo, int s_hi) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lanes = blockDim.x;
   const int gpb = lanes / G;
   const int grp = threadIdx.x / G;
   const int lane = threadIdx.x % G;
   const unsigned gmask = group_mask(G);
-  constexpr size_t kProf = group_prof_bytes<V32, K, G>();
+  constexpr size_t kProf = group_prof_bytes<VT, K, G>();
   unsigned char *gbase = smem + (size_t)grp * (kProf + (size_t)bcap);
   GroupSmem gs;
   gs.prof = reinterpret_cast<uint32_t *>(gbase);
@@ -564,10 +568,11 @@ __global__ void __launch_bounds__(256) k_rev_wave(PairSet ps, ResultSet rs, Scor
   const int64_t total = *wl.wide_count < wl.cap ? *wl.wide_count : wl.cap;
   const int64_t gid = (int64_t)blockIdx.x * gpb + grp;
   const int64_t gstride = (int64_t)gridDim.x * gpb;
-  V32::Pay *bnd = scratch ? scratch + gid * (int64_t)scratch_stride : nullptr;
+  typename VT::Pay *bnd = scratch ? scratch + gid * (int64_t)scratch_stride : nullptr;
   for (int64_t i = gid; i < total; i += gstride) {
     const int64_t p = wl.wide[i];
     const int S = rs.score[p];
+    if (S < s_lo || S > s_hi) continue;
     const int ie = rs.a_end[p], je = rs.b_end[p];
     const int M2 = ie + 1;
     const long long dmax = M2 < je + 1 ? M2 : je + 1;
@@ -588,7 +593,7 @@ __global__ void __launch_bounds__(256) k_rev_wave(PairSet ps, ResultSet rs, Scor
     SeqView A{ps.a_code + ps.a_off[p] + ie, -1, M2};
     SeqView B{ps.b_code + ps.b_off[p] + je, -1, N2};
     SweepOut so;
-    sweep_pair<V32, K, G>(A, B, sc, gs, lane, gmask, bnd, 0x7fffffff, so);
+    sweep_pair<VT, K, G>(A, B, sc, gs, lane, gmask, bnd, 0x7fffffff, so);
     if (lane == 0) {
       if (key_value(so.key) != S) {
         rs.flag[p] |= kFlagTooLong;
@@ -834,6 +839,60 @@ cudaError_t join_from(const Forks &f, cudaStream_t st, int k) {
   return e;
 }
 
+
+// Strip plan of a wavefront launch: the grid and the boundary scratch its groups need
+// when A is longer than one strip (max_a > 2*K*G).  Returns false when that scratch is
+// not available.
+template <class VT>
+static bool wave_plan(FwdConfig &c, int max_a, void *scratch, size_t scratch_bytes, int sms,
+                      typename VT::Pay **scr) {
+  *scr = nullptr;
+  if (max_a > 2 * c.K * c.G) {
+    const size_t per_group = (size_t)c.bcap * sizeof(typename VT::Pay);
+    const int groups =
+        scratch ? (int)std::min<size_t>(scratch_bytes / per_group, (size_t)c.grid * c.groups_per_block) : 0;
+    if (groups < c.groups_per_block) return false;
+    c.grid = groups / c.groups_per_block;
+    *scr = reinterpret_cast<typename VT::Pay *>(scratch);
+  }
+  c.grid = std::max(1, std::min(c.grid, sms * 4));
+  return true;
+}
+
+template <class VT>
+static bool wave_launch_ok(FwdConfig c, int max_a, void *scratch, size_t scratch_bytes, int sms) {
+  typename VT::Pay *scr;
+  return wave_plan<VT>(c, max_a, scratch, scratch_bytes, sms, &scr);
+}
+
+template <class VT, int K>
+static cudaError_t launch_rev_wave_t(FwdConfig c, const PairSet &ps, const ResultSet &rs, const Scoring &sc,
+                                     const WorkLists &wl, void *scratch, size_t scratch_bytes, int max_a, int sms,
+                                     int s_lo, int s_hi, cudaStream_t st) {
+  typename VT::Pay *scr = nullptr;
+  // without scratch, pairs longer than a strip are reported (kFlagTooLong), as before
+  wave_plan<VT>(c, max_a, scratch, scratch_bytes, sms, &scr);
+  auto kern = k_rev_wave<VT, K, kG>;
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void *>(kern), c.smem);
+  if (e != cudaSuccess) return e;
+  kern<<<c.grid, c.groups_per_block * kG, c.smem, st>>>(ps, rs, sc, wl, scr, c.bcap, c.pad, c.bcap, s_lo, s_hi);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_rev_wave16(const FwdConfig &c, const PairSet &ps, const ResultSet &rs, const Scoring &sc,
+                                     const WorkLists &wl, void *scratch, size_t scratch_bytes, int max_a, int sms,
+                                     cudaStream_t st) {
+  switch (c.K) {
+    case 2: return launch_rev_wave_t<V16, 2>(c, ps, rs, sc, wl, scratch, scratch_bytes, max_a, sms, 1, kWaveScore16, st);
+    case 3: return launch_rev_wave_t<V16, 3>(c, ps, rs, sc, wl, scratch, scratch_bytes, max_a, sms, 1, kWaveScore16, st);
+    case 4: return launch_rev_wave_t<V16, 4>(c, ps, rs, sc, wl, scratch, scratch_bytes, max_a, sms, 1, kWaveScore16, st);
+    case 5: return launch_rev_wave_t<V16, 5>(c, ps, rs, sc, wl, scratch, scratch_bytes, max_a, sms, 1, kWaveScore16, st);
+    case 6: return launch_rev_wave_t<V16, 6>(c, ps, rs, sc, wl, scratch, scratch_bytes, max_a, sms, 1, kWaveScore16, st);
+    case 7: return launch_rev_wave_t<V16, 7>(c, ps, rs, sc, wl, scratch, scratch_bytes, max_a, sms, 1, kWaveScore16, st);
+    default: return launch_rev_wave_t<V16, 8>(c, ps, rs, sc, wl, scratch, scratch_bytes, max_a, sms, 1, kWaveScore16, st);
+  }
+}
+
 cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, const Scoring &sc, int max_a,
                            int max_b, void *scratch, size_t scratch_bytes, const WorkLists &wl, cudaStream_t st,
                            const uint32_t *order, const Forks *fk) {
@@ -881,27 +940,20 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
       if (e != cudaSuccess) return e;
     }
   }
-  // Wide bands: wavefront on the reversed box (count read on the device).
-  FwdConfig c;
-  cudaError_t e = plan_forward(device, max_a, max_b, true, &c);
+  // Wide bands: wavefront on the reversed box (count read on the device), in int16 for
+  // scores up to kWaveScore16 where a strip plan with scratch exists, int32 otherwise.
+  FwdConfig c16, c32;
+  cudaError_t e = plan_forward(device, max_a, max_b, false, &c16, false, false);
   if (e != cudaSuccess) return e;
-  const int RS = 2 * c.K * c.G;
-  int stride = c.bcap;
-  V32::Pay *scr = nullptr;
-  if (max_a > RS) {
-    size_t per_group = (size_t)stride * sizeof(V32::Pay);
-    int groups = scratch ? (int)std::min<size_t>(scratch_bytes / per_group, (size_t)c.grid * c.groups_per_block) : 0;
-    if (groups >= c.groups_per_block) {
-      c.grid = groups / c.groups_per_block;
-      scr = reinterpret_cast<V32::Pay *>(scratch);
-    }
+  e = plan_forward(device, max_a, max_b, true, &c32);
+  if (e != cudaSuccess) return e;
+  int split = 0;  // largest score the int16 launch takes
+  if (wave_launch_ok<V16>(c16, max_a, scratch, scratch_bytes, sms)) {
+    e = launch_rev_wave16(c16, ps, rs, sc, wl, scratch, scratch_bytes, max_a, sms, st);
+    if (e != cudaSuccess) return e;
+    split = kWaveScore16;
   }
-  c.grid = std::max(1, std::min(c.grid, sms * 4));
-  auto kern = k_rev_wave<4, kG>;
-  e = raise_smem_limit(reinterpret_cast<const void *>(kern), c.smem);
-  if (e != cudaSuccess) return e;
-  kern<<<c.grid, c.groups_per_block * kG, c.smem, st>>>(ps, rs, sc, wl, scr, stride, c.pad, c.bcap);
-  return cudaGetLastError();
+  return launch_rev_wave_t<V32, 4>(c32, ps, rs, sc, wl, scratch, scratch_bytes, max_a, sms, split + 1, 0x7fffffff, st);
 }
 
 cudaError_t raise_smem_limit(const void *func, size_t bytes) {
