@@ -61,7 +61,8 @@ def test_dropin_protocol_klign(gpu):
 @pytest.mark.parametrize("cfg", [1, 2])
 def test_penalties_above_gap_open(built, sc, cfg):
     """A mismatch or ambiguity penalty above the gap-open penalty: the forward pass takes
-    the generic int32 engine and the begin pass the band kernels' offset-128 score table."""
+    the generic engine (not the keyed one) and the begin pass the band kernels' offset-128
+    score table."""
     m, x, go, ge, amb = sc
     d = GPUDriver()
     d.init(0, 1, m, -x, -go, -ge, 0)
