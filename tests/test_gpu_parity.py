@@ -106,6 +106,40 @@ def test_long_a_strips(built):
     assert not _diff(got, want, pairs)
 
 
+def test_high_scores_long_near_identical_pairs(built):
+    """Near-identical 20,000-base pairs with about 20 substitutions and an indel: scores
+    above 16,000 whose gap bound exceeds the widest begin band, so the begin search takes
+    the int32 wavefront on the reversed box; and a 33,000-base pair whose score passes
+    32,767, beyond SSW's 16-bit range (the oracle is int32)."""
+    import random
+
+    rng = random.Random(11)
+
+    def mutate(x, subs, indel):
+        y = list(x)
+        for _ in range(subs):
+            k = rng.randrange(len(y))
+            y[k] = rng.choice([c for c in "ACGT" if c != y[k]])
+        if indel:
+            del y[rng.randrange(len(y))]
+        return "".join(y)
+
+    a, b = [], []
+    for n, subs in ((20000, 20), (20000, 24), (20000, 30), (33000, 3)):
+        x = "".join(rng.choice("ACGT") for _ in range(n))
+        a.append(x)
+        b.append(mutate(x, subs, True))
+    pairs = Pairs.from_lists(a, b)
+    want = oracle.align_batch(pairs, SC, 4)
+    assert want[:3, 0].min() > 16000 and want[3, 0] > 32767
+    d = GPUDriver()
+    d.init(0, 1, 1, -3, -5, -2, 0)
+    d.set_ambiguity(-2)
+    for form in (FORM_PLAIN, FORM_BATCHED):
+        got = d.align_pairs(pairs, form=form)
+        assert not _diff(got, want)
+
+
 def test_edge_cases(gpu):
     cases = [
         (b"A", b"A"), (b"A", b"C"), (b"N", b"N"), (b"ACGT", b"acgt"), (b"UUUU", b"AAAA"),
