@@ -354,9 +354,9 @@ def _protein_pairs(n: int, seed: int = 8):
     """Seeded protein pairs: A of U[100, 500] residues; B = A with 10% substitutions and 2%
     deletions between random flanks (one pair in three unrelated)."""
     from mhm2_staging_gb300 import Pairs
-    from oracle import oracle
+    from mhm2_staging_gb300.protein import PROTEIN_LETTERS
 
-    letters = np.frombuffer(oracle.PROTEIN_LETTERS.encode(), dtype=np.uint8)
+    letters = np.frombuffer(PROTEIN_LETTERS.encode(), dtype=np.uint8)
     rng = np.random.default_rng(seed)
     a, b = [], []
     for k in range(n):
@@ -381,14 +381,14 @@ def _protein_path(n: int = 100_000) -> dict:
     clock, synchronous call).  GCUPS count the forward cells.  Beside it the oracle port
     on the first 20,000 pairs."""
     from mhm2_staging_gb300 import GPUDriver
-    from oracle import oracle
+    from mhm2_staging_gb300.protein import protein_encoding
 
     pairs = _protein_pairs(n)
     rng = np.random.default_rng(2024)
     m = rng.integers(-4, 4, (24, 24))
     m = (np.triu(m) + np.triu(m, 1).T).astype(np.int16)
     np.fill_diagonal(m, rng.integers(4, 12, 24))
-    enc = oracle.protein_encoding()
+    enc = protein_encoding()
     d = GPUDriver()
     d.init(0, 1, 1, -1, -11, -1, 0)
     d.align_protein(pairs, m, enc)
@@ -397,6 +397,8 @@ def _protein_path(n: int = 100_000) -> dict:
         d.align_protein(pairs, m, enc)
     dt = (time.perf_counter() - t0) / 3
     cells = float(pairs.cells())
+    from oracle import oracle  # the CPU baseline beside the path line
+
     sub = pairs.slice(0, 20_000)
     t0 = time.perf_counter()
     oracle.protein_batch(sub, m, enc, 11, 1, os.cpu_count() or 1)
