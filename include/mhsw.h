@@ -356,7 +356,8 @@ typedef struct {   /* host pointers, n each: klign's Aln fields */
   int32_t *cigar_slot;        /* may be NULL.  In CIGAR mode: the candidate's index in the CIGAR
                                * batch mhsw_last_cigar then returns (the aligned candidates), -1
                                * for a perfect match, whose SAM CIGAR klign writes as
-                               * "<rstop - rstart>=" with 0 mismatches (src/klign.cpp:229) */
+                               * "<rstop - rstart>=" with 0 mismatches (src/klign.cpp:229);
+                               * left unwritten outside CIGAR mode */
 } mhsw_alns;
 
 /* Runs the whole caller side plus the alignments for a candidate batch with the driver's
