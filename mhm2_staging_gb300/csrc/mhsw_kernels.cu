@@ -270,9 +270,33 @@ __global__ void __launch_bounds__(256) k_rev_scatter(ResultSet rs, Scoring sc, c
       for (int k = kBandClasses - 1; k >= 0; k--)
         if (g <= band_half(k)) c = k;
     }
-    append_agg(wl.wide, wl.wide_count, wl.cap, p, c == kBandClasses);
+    // one append per class present in the warp: lanes of a class share one atomic
+    const unsigned act = __activemask();
+    const unsigned same = __match_any_sync(act, c);
+    const int lane32 = threadIdx.x & 31;
+    const int leader = __ffs(same) - 1;
+    int64_t *list = nullptr;
+    int *cnt = nullptr;
+    int64_t cap = 0;
+    if (c == kBandClasses) {
+      list = wl.wide;
+      cnt = wl.wide_count;
+      cap = wl.cap;
+    } else if (c >= 0) {
+      int o = 0;
 #pragma unroll
-    for (int k = 0; k < kBandClasses; k++) append_agg(wl.bands + off[k], cursor + k, wl.cap - off[k], p, c == k);
+      for (int k = 0; k < kBandClasses; k++) o = k == c ? off[k] : o;
+      list = wl.bands + o;
+      cnt = cursor + c;
+      cap = wl.cap - o;
+    }
+    int base = 0;
+    if (c >= 0 && lane32 == leader) base = atomicAdd(cnt, __popc(same));
+    base = __shfl_sync(act, base, leader);
+    if (c >= 0) {
+      const int slot = base + __popc(same & ((1u << lane32) - 1u));
+      if (slot < cap) list[slot] = p;
+    }
   }
 }
 
