@@ -31,7 +31,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 SCORING = (1, 3, 5, 2, 2)  # match, mismatch, gap open, gap extend, ambiguity (magnitudes)
-K_OPS_PER_CELL_PAIR = 6     # packed int16x2 ops per two cell updates
+# packed int16x2 ops per two cell updates in the minimal recurrence: H - gO; the E and F
+# add-max updates; diagonal + profile; the 3-way max with relu; the max tracking
+K_OPS_PER_CELL_PAIR = 6
 WORKLOAD_NAME = "uneven read/ref lengths, 4M pairs (60% 150bp, 30% 250bp, 10% U[50,150]bp; ref lognormal(ln400,0.6) in [64,2048])"
 
 

@@ -34,7 +34,7 @@ def test_config1_shape():
     assert 0.0005 < n_frac < 0.002
 
 
-def test_config2_shape():
+def test_uneven_workload_shape():
     p = workloads.generate(2, n=40000)
     frac150 = (p.a_len == 150).mean()
     frac250 = (p.a_len == 250).mean()
