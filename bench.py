@@ -465,7 +465,7 @@ def main() -> None:
     ap.add_argument("--ref-pairs", type=int, default=200000, help="pairs per step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-paths", action="store_true", help="skip the per-workload path measurements")
     ap.add_argument("--cigar", action="store_true",
                     help="CIGAR mode in the timed regions (SSW's report_cigar output as well; e2e copies it back)")
@@ -611,6 +611,22 @@ def main() -> None:
     houts = [hout, pinned(np.zeros((pairs.n, 5), dtype=np.int32))]
     for o in houts:
         drv.align_pairs(hp, form=FORM_BATCHED, out=o, hints=True)  # warm (sizes both input sets)
+    # this host's copy rate: the step's sequence bytes, pinned host -> device, one plain copy
+    # (it varies between hosts; the pipelined e2e hides it while it stays below the kernels')
+    hseq = pinned.keep[0]  # the pinned tensor behind hp.a_seq
+    assert hseq.is_pinned() and hseq.data_ptr() == hp.a_seq.ctypes.data
+    dseq = torch.empty_like(hseq, device=dev)
+    c0 = torch.cuda.Event(enable_timing=True)
+    c1 = torch.cuda.Event(enable_timing=True)
+    dseq.copy_(hseq, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    c0.record(stream)
+    with torch.cuda.stream(stream):
+        dseq.copy_(hseq, non_blocking=True)
+    c1.record(stream)
+    torch.cuda.synchronize(dev)
+    h2d_gbs = hseq.numel() / (c0.elapsed_time(c1) * 1e-3) / 1e9
+    del dseq
     barrier()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
@@ -691,6 +707,7 @@ def main() -> None:
             "fwd_ms": statistics.mean(fwd_ms), "rev_ms": statistics.mean(rev_ms),
             "plain": plain, "batched_vs_plain": (gcups / plain["gcups"]) if plain else None,
             "e2e": {"value": e2e_gcups, "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "host_to_device_gbs": h2d_gbs,
                     "ms_per_step": e2e_s * 1e3, "steps": args.e2e_steps,
                     "mode": "async calls, two in flight: step k+1's copies overlap step k's kernels"},
             "e2e_sequential": {"value": cells_all / e2e_seq_s / 1e9, "unit": "GCUPS", "ms_per_step": e2e_seq_s * 1e3,
