@@ -74,6 +74,26 @@ def test_penalties_above_gap_open(built, sc, cfg):
         assert not _diff(got, want, pairs)
 
 
+@pytest.mark.parametrize("seed", range(12))
+def test_random_scorings(built, seed):
+    """Randomly drawn scorings (match 1-4, mismatch 1-8, gap open 1-10, gap extend 1-10,
+    ambiguity 0-6): the keyed or the generic forward engine, the biased or the offset-128
+    band table, as each scoring selects; both forms against the oracle."""
+    import random
+
+    rng = random.Random(1000 + seed)
+    sc = (rng.randint(1, 4), rng.randint(1, 8), rng.randint(1, 10), rng.randint(1, 10), rng.randint(0, 6))
+    m, x, go, ge, amb = sc
+    d = GPUDriver()
+    d.init(0, 1, m, -x, -go, -ge, 0)
+    d.set_ambiguity(-amb)
+    pairs = workloads.generate(1 if seed % 2 else 2, n=3000, seed=seed)
+    want = oracle.align_batch(pairs, sc)
+    for form in (FORM_PLAIN, FORM_BATCHED):
+        got = d.align_pairs(pairs, form=form)
+        assert not _diff(got, want, pairs), (sc, form)
+
+
 def test_forced_int32_rerun(built):
     d = GPUDriver()
     d.init(0, 1, 1, -3, -5, -2, 300)
