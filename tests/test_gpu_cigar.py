@@ -92,6 +92,20 @@ def test_cigar_adversarial(built, scoring):
     assert t["cigar_ms"] > 0
 
 
+@pytest.mark.parametrize("seed", range(8))
+def test_cigar_random_scorings(built, seed):
+    """Randomly drawn scorings (match 1-4, mismatch 1-8, gap open 1-10, gap extend 1-10,
+    ambiguity 0-6) on adversarial and uneven pairs: the register band kernels where the
+    lazy-F identity holds (gap open >= gap extend), the generic kernel elsewhere."""
+    rng = random.Random(2000 + seed)
+    sc = (rng.randint(1, 4), rng.randint(1, 8), rng.randint(1, 10), rng.randint(1, 10), rng.randint(0, 6))
+    adv = _adversarial(2500, 100 + seed)
+    unev = workloads.generate(2, n=1500, seed=seed)
+    a = [adv.a(i) for i in range(adv.n)] + [unev.a(i) for i in range(unev.n)]
+    b = [adv.b(i) for i in range(adv.n)] + [unev.b(i) for i in range(unev.n)]
+    _check(_driver(sc), Pairs.from_lists(a, b), sc, FORM_PLAIN if seed % 2 else FORM_BATCHED)
+
+
 def test_cigar_long_boxes_take_the_generic_kernel(built):
     """Boxes longer than the register kernels' row capacity (512): 600-2000 bp reads
     against their own mutated copies."""
