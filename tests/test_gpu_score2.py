@@ -43,6 +43,21 @@ def test_score2_matches_oracle(built, cfg, n, form):
     assert not _diff(_run(_driver(), pairs, form), want)
 
 
+@pytest.mark.parametrize("seed", range(8))
+def test_score2_random_scorings(built, seed):
+    """Randomly drawn scorings (match 1-4, mismatch 1-8, gap open 1-10, gap extend 1-10,
+    ambiguity 0-6): SSW's byte or word path (its bias is the largest penalty of the
+    substitution matrix) per pair, both forms, against the oracle."""
+    import random
+
+    rng = random.Random(3000 + seed)
+    sc = (rng.randint(1, 4), rng.randint(1, 8), rng.randint(1, 10), rng.randint(1, 10), rng.randint(0, 6))
+    pairs = workloads.generate(1 if seed % 2 else 2, n=2500, seed=seed)
+    want = oracle.align_batch(pairs, sc, score2=True)
+    for form in (FORM_PLAIN, FORM_BATCHED):
+        assert not _diff(_run(_driver(sc), pairs, form), want), (sc, form)
+
+
 @pytest.mark.parametrize("form", [FORM_PLAIN, FORM_BATCHED])
 def test_score2_word_path_and_int32(built, form):
     """Match 2 on 250 bp reads: scores past 255 - bias take SSW's word path (padding to a
