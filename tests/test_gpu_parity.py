@@ -160,6 +160,35 @@ def test_high_scores_long_near_identical_pairs(built):
         assert not _diff(got, want)
 
 
+def test_size_limits(built):
+    """B of exactly the largest length the kernels take, in both forms, bit-exact; one byte
+    more is refused with the limit error and the handle stays usable; A has no limit
+    (strips): a 70,000-base A against a short B."""
+    import random
+
+    from mhm2_staging_gb300.driver import limits
+
+    rng = random.Random(5)
+    lim = limits().max_b_len
+    read = "".join(rng.choice("ACGT") for _ in range(150))
+    flank = "".join(rng.choice("ACGT") for _ in range(lim - 150))
+    window = flank[: lim // 2] + read[:70] + "T" + read[71:] + flank[lim // 2:]
+    assert len(window) == lim
+    long_a = "".join(rng.choice("ACGT") for _ in range(70000))
+    pairs = Pairs.from_lists([read, read, long_a], [window, read[::-1], long_a[30000:30200]])
+    want = oracle.align_batch(pairs, SC)
+    d = GPUDriver()
+    d.init(0, 1, 1, -3, -5, -2, 0)
+    d.set_ambiguity(-2)
+    for form in (FORM_PLAIN, FORM_BATCHED):
+        assert not _diff(d.align_pairs(pairs, form=form), want, pairs)
+    too_long = Pairs.from_lists([read], [window + "A"])
+    for form in (FORM_PLAIN, FORM_BATCHED):
+        with pytest.raises(RuntimeError):
+            d.align_pairs(too_long, form=form)
+    assert not _diff(d.align_pairs(pairs, form=FORM_BATCHED), want, pairs)
+
+
 def test_edge_cases(gpu):
     cases = [
         (b"A", b"A"), (b"A", b"C"), (b"N", b"N"), (b"ACGT", b"acgt"), (b"UUUU", b"AAAA"),
