@@ -427,6 +427,20 @@ def _klign_caller_path(drv, n: int = 200_000) -> dict:
     for _ in range(3):
         r = klign_align(drv, rc, cand)
     dt = (time.perf_counter() - t0) / 3
+    # klign's SAM run: CIGAR mode at its post-assembly scoring (src/klign.cpp:1061-1064),
+    # the SAM CIGAR strings and mismatches built on the host from the returned ops
+    from mhm2_staging_gb300 import FORM_BATCHED, GPUDriver
+
+    dc = GPUDriver()
+    dc.init(0, 1, 2, -4, -4, -2, 0)
+    dc.set_ambiguity(-1)
+    dc.set_form(FORM_BATCHED)
+    dc.set_cigar(True)
+    rcg = klign_align(dc, rc, cand, cigar_ops=True)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        rcg = klign_align(dc, rc, cand, cigar_ops=True)
+    dtc = (time.perf_counter() - t0) / 3
     rc.close()
     sub = cand.slice(0, 20_000)
     t0 = time.perf_counter()
@@ -436,6 +450,11 @@ def _klign_caller_path(drv, n: int = 200_000) -> dict:
     cdt = time.perf_counter() - t0
     return {"candidates_per_s": n / dt, "ms_per_call": dt * 1e3, "candidates": n, "aligned": r["n_aligned"],
             "perfect_fraction": float(r["perfect"].mean()),
+            "cigar_mode": {"candidates_per_s": n / dtc, "ms_per_call": dtc * 1e3, "scoring": [2, 4, 4, 2, 1],
+                           "aligned": rcg["n_aligned"],
+                           "cigar_ops": int(rcg["cigar_batch"].op_off[-1]),
+                           "note": "each aligned candidate's BAM-encoded CIGAR ops and mismatches in host "
+                                   "arrays (perfect matches: <overlap>=)"},
             "cpu_port": {"candidates_per_s": sub.n / cdt, "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": f"first {sub.n} candidates ({cdt:.1f} s)"}}
 

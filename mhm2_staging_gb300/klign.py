@@ -73,10 +73,13 @@ class ResidentContigs:
         self.close()
 
 
-def klign_align(drv: "D.GPUDriver", rc: ResidentContigs, cand: Candidates, cigars: bool = False) -> dict:
+def klign_align(drv: "D.GPUDriver", rc: ResidentContigs, cand: Candidates, cigars: bool = False,
+                cigar_ops: bool = False) -> dict:
     """Aln fields per candidate (rstart, rstop, cstart, cstop, score1, score2, identity,
     orient as b'+'/b'-' codes, perfect) and n_aligned, as mhsw_klign_align computes them;
-    with cigars (the driver in CIGAR mode) also klign's SAM CIGAR string and mismatches."""
+    with cigars (the driver in CIGAR mode) also klign's SAM CIGAR string and mismatches;
+    with cigar_ops the same as arrays: cigar_slot (index into the batch, -1 for a perfect
+    match) and cigar_batch (driver.Cigars of the aligned candidates)."""
     n = cand.n
     arrs = {k: np.zeros(n, dtype=np.int32) for k in ("rstart", "rstop", "cstart", "cstop", "score1", "score2",
                                                      "identity")}
@@ -88,10 +91,14 @@ def klign_align(drv: "D.GPUDriver", rc: ResidentContigs, cand: Candidates, cigar
     ct = D.CandidatesT(cand.read_seq.ctypes.data, *(k.ctypes.data for k in keep), n, cand.kmer_len)
     slot = np.full(n, -1, dtype=np.int32)
     at = D.AlnsT(*(arrs[k].ctypes.data for k in ("rstart", "rstop", "cstart", "cstop", "score1", "score2",
-                                                  "identity", "orient", "perfect")), slot.ctypes.data if cigars else None)
+                                                  "identity", "orient", "perfect")),
+                   slot.ctypes.data if cigars or cigar_ops else None)
     m = C.c_int64(0)
     drv._ck(drv._lib.mhsw_klign_align(drv._h, rc.handle, C.byref(ct), C.byref(at), C.byref(m)), "klign_align")
     arrs["n_aligned"] = int(m.value)
+    if cigar_ops and not cigars:
+        arrs["cigar_slot"] = slot
+        arrs["cigar_batch"] = drv.last_cigar(arrs["n_aligned"])
     if cigars:
         # klign's SAM fields: "<overlap>=" and 0 mismatches for a perfect match (src/klign.cpp:229),
         # SSW's cigar_string and mismatches for the aligned candidates

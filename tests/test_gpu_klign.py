@@ -105,3 +105,17 @@ def test_klign_caller_sam_cigars(contigs, resident):
     bad = [i for i in range(cand.n) if got["cigar"][i] != want["cigar"][i]]
     assert not bad, (len(bad), got["cigar"][bad[0]], want["cigar"][bad[0]])
     assert np.array_equal(got["mismatches"], want["mismatches"])
+
+
+def test_klign_caller_cigar_ops_arrays(contigs, resident):
+    """The array form of CIGAR mode (cigar_ops) returns the batch the strings come from."""
+    sc = (2, 4, 4, 2, 1)
+    cand = generate_candidates(contigs, 3000, seed=35)
+    d = _driver(sc)
+    d.set_cigar(True)
+    got = klign_align(d, resident, cand, cigar_ops=True)
+    s = klign_align(d, resident, cand, cigars=True)
+    slot, cb = got["cigar_slot"], got["cigar_batch"]
+    strings = [cb.string(int(j)) if j >= 0 else f"{got['rstop'][i] - got['rstart'][i]}=" for i, j in enumerate(slot)]
+    assert strings == s["cigar"]
+    assert got["n_aligned"] == s["n_aligned"] and len(cb.nops) == got["n_aligned"]
