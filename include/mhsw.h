@@ -67,7 +67,10 @@ typedef struct {
   int32_t *score2_32, *a_end2_32;
 } mhsw_aln_results;
 
-/* Device-timed figures of the last mhsw_align_pairs / run_kernel_* call. */
+/* Device-timed figures of the last mhsw_align_pairs / run_kernel_* call, or of the
+ * aligned candidates of the last mhsw_klign_align call (n_pairs = those aligned; total_ms
+ * from their translation to the end of the begin pass; fwd_cells and the counters of
+ * re-runs left 0). */
 typedef struct {
   double fwd_ms;      /* forward kernels (incl. int32 re-runs) */
   double rev_ms;      /* begin (reverse) kernels */

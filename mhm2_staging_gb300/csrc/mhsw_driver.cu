@@ -1592,19 +1592,37 @@ int align_resident(mhsw_driver *d, const PairSet &in, int64_t a_bytes, int max_a
   rc = ensure_results(d, n);
   if (rc) return rc;
   MHSW_CK(d->a_code.reserve((size_t)a_bytes + 16), "cudaMalloc codes");
+  MHSW_CK(cudaEventRecord(d->ev_t[0], d->st), "event");
   MHSW_CK(launch_translate(in.a_seq, d->a_code.p, a_bytes, d->st), "translate A");
   d->launches += 1;
   PairSet ps = in;
   ps.a_code = d->a_code.p;
   rc = attach_score2(d, &ps, n, a_bytes);
   if (rc) return rc;
+  MHSW_CK(cudaEventRecord(d->ev_t[1], d->st), "event");
   rc = forward_any(d, ps, max_a, max_b, form);
   if (rc) return rc;
+  MHSW_CK(cudaEventRecord(d->ev_t[2], d->st), "event");
   rc = run_reverse(d, ps, max_a, max_b, d->fwd_order);
   if (rc) return rc;
+  MHSW_CK(cudaEventRecord(d->ev_t[3], d->st), "event");
   MHSW_CK(launch_pack5(result_set(d), n, out5_dev, d->st), "pack5");
   d->launches += 1;
+  d->timing = mhsw_timing{};
+  d->timing.n_pairs = n;
   return MHSW_OK;
+}
+
+void resident_timing(mhsw_driver *d) {
+  if (!d) return;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (d->timing.n_pairs <= 0) return;
+  d->timing.fwd_ms = elapsed(d->ev_t[1], d->ev_t[2]);
+  d->timing.rev_ms = elapsed(d->ev_t[2], d->ev_t[3]);
+  d->timing.total_ms = elapsed(d->ev_t[0], d->ev_t[3]);
+  d->timing.launches = d->launches;
+  d->timing.cigar_ms = d->cigar ? d->cigar_ms : 0;
+  d->timing.n_cigar_generic = d->cigar ? d->cigar_generic : 0;
 }
 
 void *driver_stream(mhsw_driver *d) { return d ? static_cast<void *>(d->st) : nullptr; }

@@ -30,6 +30,9 @@ void driver_gaps(mhsw_driver *d, int *gap_open, int *gap_extend);
 // Returns MHSW_ERR_STATE when the handle is not in CIGAR mode.
 int cigar_resident(mhsw_driver *d, const PairSet &ps);
 bool driver_cigar(mhsw_driver *d);
+// After the stream work of an align_resident call (and its CIGAR pass) completed: its
+// device times into the handle's mhsw_timing (translation to end of the begin pass).
+void resident_timing(mhsw_driver *d);
 // The A codes the last align_resident call translated (device).
 const uint8_t *driver_a_codes(mhsw_driver *d);
 // Second-best scores (device, n entries) of the last align_resident call when the handle

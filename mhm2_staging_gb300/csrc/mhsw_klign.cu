@@ -381,6 +381,7 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
     down(out->perfect, o_pf, (size_t)n);
     if (out->cigar_slot && mhsw::driver_cigar(d)) down(out->cigar_slot, slot, sizeof(int32_t) * n);
     if (!e) e = cudaStreamSynchronize(st);
+    if (!e && h_counts[0] > 0) mhsw::resident_timing(d);
   }
   for (void *p : allocs) cudaFreeAsync(p, st);
   cudaStreamSynchronize(st);

@@ -53,10 +53,13 @@ def _diff(got, want):
 @pytest.mark.parametrize("sc,score2", [((1, 3, 5, 2, 2), False), ((2, 4, 4, 2, 1), True)])
 def test_klign_caller_matches_restatement(contigs, resident, form, sc, score2):
     cand = generate_candidates(contigs, 30000, seed=21)
-    got = klign_align(_driver(sc, form, score2), resident, cand)
+    d = _driver(sc, form, score2)
+    got = klign_align(d, resident, cand)
     want = _want(contigs, cand, sc, score2)
     assert not _diff(got, want)
     assert 0.3 < got["perfect"].mean() < 0.6 and got["n_aligned"] > 10000
+    t = d.last_timing()  # the aligned candidates' device times
+    assert t["n_pairs"] == got["n_aligned"] and t["fwd_ms"] > 0 and t["total_ms"] >= t["fwd_ms"]
 
 
 def test_klign_caller_k21_and_all_reverse(contigs, resident):
