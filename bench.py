@@ -670,6 +670,7 @@ def main() -> None:
         if args.cigar:
             drv.last_cigar(pairs.n)
     e2e_seq_s = allmax((time.perf_counter() - t0) / 2)
+    seq_t = drv.last_timing()  # the last sequential call's device span (copies in, kernels, copy out)
 
     # ---- other paths of the scope: per-workload GCUPS, device-resident ----------------
     paths = None
@@ -731,7 +732,10 @@ def main() -> None:
                     "ms_per_step": e2e_s * 1e3, "steps": args.e2e_steps,
                     "mode": "async calls, two in flight: step k+1's copies overlap step k's kernels"},
             "e2e_sequential": {"value": cells_all / e2e_seq_s / 1e9, "unit": "GCUPS", "ms_per_step": e2e_seq_s * 1e3,
-                               "mode": "1 handle, one synchronous call at a time"},
+                               "device_ms": seq_t["total_ms"], "fwd_ms": seq_t["fwd_ms"], "rev_ms": seq_t["rev_ms"],
+                               "mode": "1 handle, one synchronous call at a time; device_ms = the last call's "
+                                       "device span from its first copy in to its result copy out (the rest "
+                                       "of ms_per_step is host time)"},
             "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "paths": paths,
