@@ -97,6 +97,12 @@ def test_python_mirror_raises_like_reference(built):
             d.run_kernel_forwards(["ACGT"], ["ACGT"], 4, 4)
 
 
+def test_missing_library_fails_loudly(tmp_path):
+    """No CPU fallback: without the built library the package raises instead of computing."""
+    with pytest.raises(RuntimeError, match="libmhsw.so not found"):
+        D.load_library(tmp_path / "libmhsw.so")
+
+
 @pytest.mark.skipif(shutil.which("g++") is None, reason="no C++ compiler")
 def test_cpp_dropin_header_compiles_and_links(built, tmp_path):
     src = tmp_path / "use_driver.cpp"

@@ -69,6 +69,61 @@ def test_klign_caller_k21_and_all_reverse(contigs, resident):
     assert (got["orient"] == ord("-")).all()
 
 
+def test_klign_caller_boundary_seeds_and_iupac(contigs, resident):
+    """Seeds on the first and last k-mer of the read and of the contig (windows clipped at
+    the contig's ends), reads exactly one k-mer long, and IUPAC codes and U in the reads
+    (aligned as found on '+' -- U scores as A there, the others as N -- and turned into N
+    by the reverse complement on '-')."""
+    base = generate_candidates(contigs, 4000, seed=13)
+    K, n = base.kmer_len, base.n
+    rng = np.random.default_rng(17)
+    q = np.arange(n) % 5
+    reads = [base.read_seq[o:o + L].copy() for o, L in zip(base.read_off, base.read_len)]
+    pir = base.pos_in_read.copy()
+    pic = base.pos_in_ctg.copy()
+    clen = contigs.len[base.cid]
+    for i in range(n):
+        if q[i] == 0:
+            pir[i] = 0
+        elif q[i] == 1:
+            pir[i] = len(reads[i]) - K
+        elif q[i] == 2:
+            pic[i] = 0
+        elif q[i] == 3:
+            pic[i] = clen[i] - K
+        else:  # one k-mer: the seed itself
+            reads[i] = reads[i][pir[i]:pir[i] + K].copy()
+            pir[i] = 0
+        if rng.random() < 0.15:
+            reads[i][rng.integers(0, len(reads[i]))] = np.frombuffer(b"URYKMSWBDHV", dtype=np.uint8)[rng.integers(0, 11)]
+    lens = np.array([len(r) for r in reads], dtype=np.int32)
+    off = np.zeros(n, dtype=np.int64)
+    off[1:] = np.cumsum(lens[:-1])
+    seq = np.zeros(int(lens.sum()) + 16, dtype=np.uint8)
+    for i, r in enumerate(reads):
+        seq[off[i]:off[i] + lens[i]] = r
+    cand = Candidates(seq, off, lens, base.cid.copy(), pic.astype(np.int32), pir.astype(np.int32),
+                      base.strand.copy(), K)
+    for sc, score2 in (((1, 3, 5, 2, 2), False), ((2, 4, 4, 2, 1), True)):
+        got = klign_align(_driver(sc, FORM_BATCHED, score2), resident, cand)
+        want = _want(contigs, cand, sc, score2)
+        assert not _diff(got, want)
+        assert got["perfect"][q == 4].mean() > 0.5 and got["n_aligned"] > 1000
+    assert (cand.pos_in_ctg[q == 3] + K == clen[q == 3]).all()
+    # CIGAR mode at klign's post-assembly scoring: SAM CIGARs and mismatches of the same set
+    sc = (2, 4, 4, 2, 1)
+    d = _driver(sc)
+    d.set_cigar(True)
+    got = klign_align(d, resident, cand, cigars=True)
+    want = klign_caller.klign_align(contigs.seq, contigs.off, contigs.len, cand.read_seq, cand.read_off,
+                                    cand.read_len, cand.cid, cand.pos_in_ctg, cand.pos_in_read, cand.strand,
+                                    K, sc, False, cigars=True)
+    assert not _diff(got, want)
+    bad = [i for i in range(n) if got["cigar"][i] != want["cigar"][i]]
+    assert not bad, (len(bad), got["cigar"][bad[0]], want["cigar"][bad[0]])
+    assert np.array_equal(got["mismatches"], want["mismatches"])
+
+
 def test_klign_caller_rejects_bad_candidates(contigs, resident):
     d = _driver()
     cand = generate_candidates(contigs, 10, seed=5)
