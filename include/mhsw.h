@@ -366,7 +366,9 @@ typedef struct {   /* host pointers, n each: klign's Aln fields */
 /* Runs the whole caller side plus the alignments for a candidate batch with the driver's
  * scoring, form and score2 mode; synchronous.  Fails with MHSW_ERR_ARG (nothing written)
  * when a candidate's seed lies outside its read or contig or its read has a byte revcomp
- * rejects; *n_aligned (may be NULL) receives how many candidates needed an alignment. */
+ * rejects; *n_aligned (may be NULL) receives how many candidates needed an alignment.
+ * The call's device arrays live in an arena kept on the handle (grown for a larger batch,
+ * freed with the handle), so repeated calls allocate nothing. */
 int mhsw_klign_align(mhsw_driver *drv, const mhsw_contigs *contigs, const mhsw_candidates *cand, mhsw_alns *out,
                      int64_t *n_aligned);
 

@@ -33,6 +33,10 @@ bool driver_cigar(mhsw_driver *d);
 // After the stream work of an align_resident call (and its CIGAR pass) completed: its
 // device times into the handle's mhsw_timing (translation to end of the begin pass).
 void resident_timing(mhsw_driver *d);
+// Device arena of at least `bytes` for the caller side's per-call arrays, kept on the
+// handle between calls (grown when a batch needs more, never shrunk); nullptr when the
+// allocation fails.  Its contents are only valid during one call.
+unsigned char *driver_caller_arena(mhsw_driver *d, size_t bytes);
 // The A codes the last align_resident call translated (device).
 const uint8_t *driver_a_codes(mhsw_driver *d);
 // Second-best scores (device, n entries) of the last align_resident call when the handle

@@ -189,10 +189,18 @@ __global__ void k_klign_finish(FArgs g) {
   g.perfect[c] = j < 0;
 }
 
-template <class T>
-cudaError_t dalloc(T **p, size_t n, cudaStream_t st) {
-  return cudaMallocAsync(reinterpret_cast<void **>(p), std::max<size_t>(n, 1) * sizeof(T), st);
-}
+// Lays arrays out back to back at 256-byte boundaries: with base == nullptr it only
+// sums their sizes (off), otherwise it also hands out the pointers.
+struct Carve {
+  size_t off = 0;
+  unsigned char *base = nullptr;
+  template <class T>
+  void take(T **p, size_t count) {
+    const size_t at = off;
+    off += (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~size_t(255);
+    *p = base ? reinterpret_cast<T *>(base + at) : nullptr;
+  }
+};
 
 }  // namespace
 
@@ -270,52 +278,56 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
   FArgs f{};
   int *counts = nullptr;
   int32_t *out5 = nullptr;
-  std::vector<void *> allocs;
   int rc = MHSW_OK;
   cudaError_t e = cudaSuccess;
-  auto A = [&](auto **p, size_t cnt) {
-    if (!e) e = dalloc(p, cnt, st);
-    if (!e) allocs.push_back((void *)*p);
-  };
   char *read = nullptr, *ori = nullptr;
   int64_t *roff = nullptr;
   int32_t *rlen = nullptr, *cid = nullptr, *pic = nullptr, *pir = nullptr;
   uint8_t *strand = nullptr;
-  A(&read, (size_t)rbytes + 16);
-  A(&ori, (size_t)rbytes + 16);
-  A(&roff, (size_t)n);
-  A(&rlen, (size_t)n);
-  A(&cid, (size_t)n);
-  A(&pic, (size_t)n);
-  A(&pir, (size_t)n);
-  A(&strand, (size_t)n);
   int32_t *wstart = nullptr, *rstart0 = nullptr, *ov = nullptr, *slot = nullptr;
   int8_t *orient = nullptr;
-  A(&wstart, (size_t)n);
-  A(&rstart0, (size_t)n);
-  A(&ov, (size_t)n);
-  A(&slot, (size_t)n);
-  A(&orient, (size_t)n);
   int64_t *a_off = nullptr, *b_off = nullptr;
   int32_t *a_len = nullptr, *b_len = nullptr;
-  A(&a_off, (size_t)n);
-  A(&b_off, (size_t)n);
-  A(&a_len, (size_t)n);
-  A(&b_len, (size_t)n);
-  A(&counts, 4);
   int32_t *o_rs = nullptr, *o_re = nullptr, *o_cs = nullptr, *o_ce = nullptr, *o_sc = nullptr, *o_s2 = nullptr,
           *o_id = nullptr;
   char *o_or = nullptr;
   uint8_t *o_pf = nullptr;
-  A(&o_rs, (size_t)n);
-  A(&o_re, (size_t)n);
-  A(&o_cs, (size_t)n);
-  A(&o_ce, (size_t)n);
-  A(&o_sc, (size_t)n);
-  A(&o_s2, (size_t)n);
-  A(&o_id, (size_t)n);
-  A(&o_or, (size_t)n);
-  A(&o_pf, (size_t)n);
+  // the call's arrays, laid out in the handle's caller arena (sized by a first pass)
+  auto lay = [&](Carve &c) {
+    c.take(&read, (size_t)rbytes + 16);
+    c.take(&ori, (size_t)rbytes + 16);
+    c.take(&roff, (size_t)n);
+    c.take(&rlen, (size_t)n);
+    c.take(&cid, (size_t)n);
+    c.take(&pic, (size_t)n);
+    c.take(&pir, (size_t)n);
+    c.take(&strand, (size_t)n);
+    c.take(&wstart, (size_t)n);
+    c.take(&rstart0, (size_t)n);
+    c.take(&ov, (size_t)n);
+    c.take(&slot, (size_t)n);
+    c.take(&orient, (size_t)n);
+    c.take(&a_off, (size_t)n);
+    c.take(&b_off, (size_t)n);
+    c.take(&a_len, (size_t)n);
+    c.take(&b_len, (size_t)n);
+    c.take(&counts, 4);
+    c.take(&o_rs, (size_t)n);
+    c.take(&o_re, (size_t)n);
+    c.take(&o_cs, (size_t)n);
+    c.take(&o_ce, (size_t)n);
+    c.take(&o_sc, (size_t)n);
+    c.take(&o_s2, (size_t)n);
+    c.take(&o_id, (size_t)n);
+    c.take(&o_or, (size_t)n);
+    c.take(&o_pf, (size_t)n);
+    c.take(&out5, (size_t)n * 5);  // the aligned candidates' results (at most n)
+  };
+  Carve sizing;
+  lay(sizing);
+  Carve arena{0, mhsw::driver_caller_arena(d, sizing.off)};
+  if (!arena.base) return MHSW_ERR_NOMEM;
+  lay(arena);
   auto up = [&](void *dst, const void *src, size_t bytes) {
     if (!e && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
   };
@@ -340,7 +352,6 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
   if (!e && h_counts[3] > 0) rc = MHSW_ERR_ARG;  // a read byte that revcomp rejects
   if (!e && !rc && h_counts[0] > 0) {
     const int64_t m = h_counts[0];
-    A(&out5, (size_t)m * 5);
     mhsw::PairSet ps;
     ps.a_seq = ori;
     ps.a_off = a_off;
@@ -383,8 +394,7 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
     if (!e) e = cudaStreamSynchronize(st);
     if (!e && h_counts[0] > 0) mhsw::resident_timing(d);
   }
-  for (void *p : allocs) cudaFreeAsync(p, st);
-  cudaStreamSynchronize(st);
+  if (e || rc) cudaStreamSynchronize(st);  // nothing of a failed call left in flight
   if (e) return e == cudaErrorMemoryAllocation ? MHSW_ERR_NOMEM : MHSW_ERR_CUDA;
   return rc;
 }
