@@ -664,13 +664,17 @@ def main() -> None:
     ref_out = out_dev.cpu().numpy()
     assert all(np.array_equal(o, ref_out) for o in houts), "e2e results differ from device-resident results"
     barrier()
+    seq_wall, seq_dev = [], []  # per call: wall time and device span (copies in, kernels, copy out)
     t0 = time.perf_counter()
     for _ in range(2):
+        t1 = time.perf_counter()
         drv.align_pairs(hp, form=FORM_BATCHED, out=hout, hints=True)
         if args.cigar:
             drv.last_cigar(pairs.n)
+        seq_wall.append((time.perf_counter() - t1) * 1e3)
+        seq_dev.append(drv.last_timing()["total_ms"])
     e2e_seq_s = allmax((time.perf_counter() - t0) / 2)
-    seq_t = drv.last_timing()  # the last sequential call's device span (copies in, kernels, copy out)
+    seq_t = drv.last_timing()
 
     # ---- other paths of the scope: per-workload GCUPS, device-resident ----------------
     paths = None
@@ -733,9 +737,11 @@ def main() -> None:
                     "mode": "async calls, two in flight: step k+1's copies overlap step k's kernels"},
             "e2e_sequential": {"value": cells_all / e2e_seq_s / 1e9, "unit": "GCUPS", "ms_per_step": e2e_seq_s * 1e3,
                                "device_ms": seq_t["total_ms"], "fwd_ms": seq_t["fwd_ms"], "rev_ms": seq_t["rev_ms"],
+                               "call_wall_ms": seq_wall, "call_device_ms": seq_dev,
                                "mode": "1 handle, one synchronous call at a time; device_ms = the last call's "
                                        "device span from its first copy in to its result copy out (the rest "
-                                       "of ms_per_step is host time)"},
+                                       "of ms_per_step is host time); call_* = each call's wall time and "
+                                       "device span"},
             "gpu_launches": launches,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "paths": paths,

@@ -103,7 +103,7 @@ struct mhsw_driver {
   DBuf<int> l_counts;
   DBuf<uint8_t> a_code, b_code;  // base codes of the current batch
   DBuf<unsigned char> scratch;
-  DBuf<unsigned char> caller;  // caller-side arrays (mhsw_klign_align), kept between calls
+  DBuf<unsigned char> call_arena;  // one call's own arrays (caller side, protein), kept between calls
   DBuf<unsigned char> outv;  // 5 x int16 + 5 x int32 arrays
   DBuf<int32_t> out5;
   mhsw::BatchState batch;     // batched-form work buffers
@@ -228,7 +228,7 @@ struct mhsw_driver {
     b_code.release();
     l_counts.release();
     scratch.release();
-    caller.release();
+    call_arena.release();
     outv.release();
     out5.release();
     batch.release();
@@ -1633,10 +1633,10 @@ int driver_form(mhsw_driver *d) { return d ? d->form : MHSW_FORM_PLAIN; }
 bool driver_cigar(mhsw_driver *d) { return d && d->cigar; }
 const uint8_t *driver_a_codes(mhsw_driver *d) { return d ? d->a_code.p : nullptr; }
 
-unsigned char *driver_caller_arena(mhsw_driver *d, size_t bytes) {
+unsigned char *driver_call_arena(mhsw_driver *d, size_t bytes) {
   if (!d) return nullptr;
   if (cudaSetDevice(d->device) != cudaSuccess) return nullptr;
-  return d->caller.reserve(bytes) == cudaSuccess ? d->caller.p : nullptr;
+  return d->call_arena.reserve(bytes) == cudaSuccess ? d->call_arena.p : nullptr;
 }
 
 int cigar_resident(mhsw_driver *d, const PairSet &ps) {

@@ -33,10 +33,22 @@ bool driver_cigar(mhsw_driver *d);
 // After the stream work of an align_resident call (and its CIGAR pass) completed: its
 // device times into the handle's mhsw_timing (translation to end of the begin pass).
 void resident_timing(mhsw_driver *d);
-// Device arena of at least `bytes` for the caller side's per-call arrays, kept on the
-// handle between calls (grown when a batch needs more, never shrunk); nullptr when the
-// allocation fails.  Its contents are only valid during one call.
-unsigned char *driver_caller_arena(mhsw_driver *d, size_t bytes);
+// Device arena of at least `bytes` for one call's own arrays (the caller side, the protein
+// entry point), kept on the handle between calls (grown when a batch needs more, never
+// shrunk); nullptr when the allocation fails.  Its contents are only valid during one call.
+unsigned char *driver_call_arena(mhsw_driver *d, size_t bytes);
+// Lays arrays out back to back at 256-byte boundaries: with base == nullptr it only sums
+// their sizes (off), otherwise it also hands out the pointers.
+struct Carve {
+  size_t off = 0;
+  unsigned char *base = nullptr;
+  template <class T>
+  void take(T **p, size_t count) {
+    const size_t at = off;
+    off += ((count > 0 ? count : 1) * sizeof(T) + 255) & ~size_t(255);
+    *p = base ? reinterpret_cast<T *>(base + at) : nullptr;
+  }
+};
 // The A codes the last align_resident call translated (device).
 const uint8_t *driver_a_codes(mhsw_driver *d);
 // Second-best scores (device, n entries) of the last align_resident call when the handle

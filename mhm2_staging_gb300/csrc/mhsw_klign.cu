@@ -189,18 +189,6 @@ __global__ void k_klign_finish(FArgs g) {
   g.perfect[c] = j < 0;
 }
 
-// Lays arrays out back to back at 256-byte boundaries: with base == nullptr it only
-// sums their sizes (off), otherwise it also hands out the pointers.
-struct Carve {
-  size_t off = 0;
-  unsigned char *base = nullptr;
-  template <class T>
-  void take(T **p, size_t count) {
-    const size_t at = off;
-    off += (std::max<size_t>(count, 1) * sizeof(T) + 255) & ~size_t(255);
-    *p = base ? reinterpret_cast<T *>(base + at) : nullptr;
-  }
-};
 
 }  // namespace
 
@@ -293,7 +281,7 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
   char *o_or = nullptr;
   uint8_t *o_pf = nullptr;
   // the call's arrays, laid out in the handle's caller arena (sized by a first pass)
-  auto lay = [&](Carve &c) {
+  auto lay = [&](mhsw::Carve &c) {
     c.take(&read, (size_t)rbytes + 16);
     c.take(&ori, (size_t)rbytes + 16);
     c.take(&roff, (size_t)n);
@@ -323,9 +311,9 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
     c.take(&o_pf, (size_t)n);
     c.take(&out5, (size_t)n * 5);  // the aligned candidates' results (at most n)
   };
-  Carve sizing;
+  mhsw::Carve sizing;
   lay(sizing);
-  Carve arena{0, mhsw::driver_caller_arena(d, sizing.off)};
+  mhsw::Carve arena{0, mhsw::driver_call_arena(d, sizing.off)};
   if (!arena.base) return MHSW_ERR_NOMEM;
   lay(arena);
   auto up = [&](void *dst, const void *src, size_t bytes) {

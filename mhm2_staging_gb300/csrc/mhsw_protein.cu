@@ -216,11 +216,6 @@ __global__ void k_protein_pack(const int32_t *score, const int32_t *a_beg, const
   out5[5 * p + 4] = b_end[p];
 }
 
-template <class T>
-cudaError_t dalloc(T **p, size_t n, cudaStream_t st) {
-  return cudaMallocAsync(reinterpret_cast<void **>(p), std::max<size_t>(n, 1) * sizeof(T), st);
-}
-
 }  // namespace
 
 extern "C" {
@@ -262,21 +257,48 @@ int mhsw_align_protein(mhsw_driver *d, const mhsw_pairs *pairs, const int16_t *s
     tb = std::max(tb, ob[(size_t)i] + lb[(size_t)i]);
     max_n = std::max<int64_t>(max_n, lb[(size_t)i]);
   }
-  std::vector<void *> allocs;
-  auto A = [&](auto **p, size_t cnt) {
-    if (!e) e = dalloc(p, cnt, st);
-    if (!e) allocs.push_back((void *)*p);
-  };
   char *as = nullptr, *bs = nullptr;
   int64_t *ao = nullptr, *bo = nullptr;
   int32_t *al = nullptr, *bl = nullptr;
+  uint8_t *ac = nullptr, *bc = nullptr;
+  int16_t *enc = nullptr;
+  int32_t *mat = nullptr, *sc = nullptr, *ae = nullptr, *be = nullptr, *ab = nullptr, *bb = nullptr, *o5 = nullptr;
+  int *bad = nullptr;
+  int2 *rows = nullptr;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // one warp per pair at a time; 24 resident warps per SM (76 registers x 128 threads
+  // fits 6 blocks of 4 warps) to cover the row chain's latency
+  const int64_t warps = std::min<int64_t>(n, (int64_t)sms * 24);
+  // the call's arrays, laid out in the handle's call arena (sized by a first pass)
+  auto lay = [&](mhsw::Carve &c) {
+    if (host_io) {
+      c.take(&as, (size_t)ta + 16);
+      c.take(&bs, (size_t)tb + 16);
+      c.take(&ao, (size_t)n);
+      c.take(&bo, (size_t)n);
+      c.take(&al, (size_t)n);
+      c.take(&bl, (size_t)n);
+      c.take(&o5, (size_t)n * 5);
+    }
+    c.take(&ac, (size_t)ta + 16);
+    c.take(&bc, (size_t)tb + 16);
+    c.take(&enc, kEnc);
+    c.take(&mat, kAA * kAA);
+    c.take(&sc, (size_t)n);
+    c.take(&ae, (size_t)n);
+    c.take(&be, (size_t)n);
+    c.take(&ab, (size_t)n);
+    c.take(&bb, (size_t)n);
+    c.take(&bad, 1);
+    c.take(&rows, (size_t)(warps * max_n));
+  };
+  mhsw::Carve sizing;
+  lay(sizing);
+  mhsw::Carve arena{0, mhsw::driver_call_arena(d, sizing.off)};
+  if (!arena.base) return MHSW_ERR_NOMEM;
+  lay(arena);
   if (host_io) {
-    A(&as, (size_t)ta + 16);
-    A(&bs, (size_t)tb + 16);
-    A(&ao, (size_t)n);
-    A(&bo, (size_t)n);
-    A(&al, (size_t)n);
-    A(&bl, (size_t)n);
     auto up = [&](void *dst, const void *src, size_t bytes) {
       if (!e && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
     };
@@ -293,32 +315,7 @@ int mhsw_align_protein(mhsw_driver *d, const mhsw_pairs *pairs, const int16_t *s
     bo = const_cast<int64_t *>(pairs->b_off);
     al = const_cast<int32_t *>(pairs->a_len);
     bl = const_cast<int32_t *>(pairs->b_len);
-  }
-  uint8_t *ac = nullptr, *bc = nullptr;
-  int16_t *enc = nullptr;
-  int32_t *mat = nullptr, *sc = nullptr, *ae = nullptr, *be = nullptr, *ab = nullptr, *bb = nullptr, *o5 = nullptr;
-  int *bad = nullptr;
-  int2 *rows = nullptr;
-  A(&ac, (size_t)ta + 16);
-  A(&bc, (size_t)tb + 16);
-  A(&enc, kEnc);
-  A(&mat, kAA * kAA);
-  A(&sc, (size_t)n);
-  A(&ae, (size_t)n);
-  A(&be, (size_t)n);
-  A(&ab, (size_t)n);
-  A(&bb, (size_t)n);
-  A(&bad, 1);
-  int sms = 152;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  // one warp per pair at a time; 24 resident warps per SM (76 registers x 128 threads
-  // fits 6 blocks of 4 warps) to cover the row chain's latency
-  const int64_t warps = std::min<int64_t>(n, (int64_t)sms * 24);
-  A(&rows, (size_t)(warps * max_n));
-  if (!host_io) {
     o5 = out5;
-  } else {
-    A(&o5, (size_t)n * 5);
   }
   int32_t hmat[kAA * kAA];
   for (int k = 0; k < kAA * kAA; k++) hmat[k] = scoring_matrix[k];
@@ -344,8 +341,7 @@ int mhsw_align_protein(mhsw_driver *d, const mhsw_pairs *pairs, const int16_t *s
   int hbad = 0;
   if (!e) e = cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (!e) e = cudaStreamSynchronize(st);
-  for (void *p : allocs) cudaFreeAsync(p, st);
-  cudaStreamSynchronize(st);
+  if (e) cudaStreamSynchronize(st);  // nothing of a failed call left in flight
   if (e) return e == cudaErrorMemoryAllocation ? MHSW_ERR_NOMEM : MHSW_ERR_CUDA;
   return hbad ? MHSW_ERR_ARG : MHSW_OK;
 }
