@@ -91,52 +91,109 @@ struct KArgs {
   int *counts;       // [0] list length, [1] longest read, [2] longest window, [3] bad reads
 };
 
-__global__ void k_klign_prepare(KArgs g) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= g.n) return;
-  const int rlen = g.read_len[c];
-  const int64_t ro = g.read_off[c];
-  const char *r = g.read + ro;
-  const int id = g.cid[c];
-  const bool minus = ((g.strand[c] >> 1) & 1u) != (g.strand[c] & 1u);
-  // the oriented read (klign reverse-complements every read up front, :673)
-  bool bad = false;
-  for (int t = 0; t < rlen; t++) {
-    const int cc = comp_base((unsigned char)r[rlen - 1 - t]);
-    bad |= cc < 0;
-    g.ori[ro + t] = minus ? (char)cc : r[t];
-  }
-  if (bad) atomicAdd(&g.counts[3], 1);
+// One warp per candidate, kPrepWarps candidates per block per round: the warp's lanes
+// stride the read and the window 32 bytes at a time (coalesced), the perfect-match compare
+// stops at the first round with a differing byte (a warp vote), and the block reserves its
+// aligned candidates' list slots with one atomic per round; the longest read and window
+// and the bad-read flag are reduced per block.
+constexpr int kPrepWarps = 8;
+
+__global__ void __launch_bounds__(kPrepWarps * 32) k_klign_prepare(KArgs g) {
+  __shared__ int s_need[kPrepWarps];
+  __shared__ int s_base;
+  __shared__ int s_max[3][kPrepWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
   const int K = g.kmer_len;
-  const int pos_in_read = minus ? rlen - (K + g.pir[c]) : g.pir[c];
-  const int pos_in_ctg = g.pic[c];
-  const int cl = g.clen[id];
-  const int left = min(pos_in_read, pos_in_ctg);
-  const int right = min(rlen - K - pos_in_read, cl - pos_in_ctg - K);
-  const int cstart = pos_in_ctg - left, rstart = pos_in_read - left, ov = left + K + right;
-  g.wstart[c] = cstart;
-  g.rstart0[c] = rstart;
-  g.overlap[c] = ov;
-  g.orient[c] = minus ? '-' : '+';
-  // perfect match: the window's bytes equal the oriented read's overlap (:220)
-  const char *cw = g.craw + g.coff[id] + cstart;
-  bool same = true;
-  for (int t = 0; t < ov && same; t++) {
-    const char rb = minus ? (char)comp_base((unsigned char)r[rlen - 1 - (rstart + t)]) : r[rstart + t];
-    same = cw[t] == rb;
+  int rmax = 0, omax = 0, nbad = 0;  // this warp's, kept by every lane
+  for (int64_t base = (int64_t)blockIdx.x * kPrepWarps; base < g.n; base += (int64_t)gridDim.x * kPrepWarps) {
+    const int64_t c = base + warp;
+    bool need = false;
+    int64_t ro = 0, boff = 0;
+    int rlen = 0, ov = 0;
+    if (c < g.n) {
+      rlen = g.read_len[c];
+      ro = g.read_off[c];
+      const char *r = g.read + ro;
+      const int id = g.cid[c];
+      const bool minus = ((g.strand[c] >> 1) & 1u) != (g.strand[c] & 1u);
+      // the oriented read (klign reverse-complements every read up front, :673)
+      bool bad = false;
+      for (int t = lane; t < rlen; t += 32) {
+        const int cc = comp_base((unsigned char)r[rlen - 1 - t]);
+        bad |= cc < 0;
+        g.ori[ro + t] = minus ? (char)cc : r[t];
+      }
+      if (__any_sync(full, bad)) nbad = 1;
+      const int pos_in_read = minus ? rlen - (K + g.pir[c]) : g.pir[c];
+      const int pos_in_ctg = g.pic[c];
+      const int cl = g.clen[id];
+      const int left = min(pos_in_read, pos_in_ctg);
+      const int right = min(rlen - K - pos_in_read, cl - pos_in_ctg - K);
+      const int cstart = pos_in_ctg - left, rstart = pos_in_read - left;
+      ov = left + K + right;
+      boff = g.coff[id] + cstart;
+      if (lane == 0) {
+        g.wstart[c] = cstart;
+        g.rstart0[c] = rstart;
+        g.overlap[c] = ov;
+        g.orient[c] = minus ? '-' : '+';
+      }
+      // perfect match: the window's bytes equal the oriented read's overlap (:220)
+      const char *cw = g.craw + boff;
+      for (int t0 = 0; t0 < ov; t0 += 32) {
+        const int t = t0 + lane;
+        bool ok = true;
+        if (t < ov) {
+          const char rb = minus ? (char)comp_base((unsigned char)r[rlen - 1 - (rstart + t)]) : r[rstart + t];
+          ok = cw[t] == rb;
+        }
+        if (!__all_sync(full, ok)) {
+          need = true;
+          break;
+        }
+      }
+      if (need) {
+        rmax = max(rmax, rlen);
+        omax = max(omax, ov);
+      } else if (lane == 0) {
+        g.slot[c] = -1;
+      }
+    }
+    if (lane == 0) s_need[warp] = need ? 1 : 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < kPrepWarps; w++) tot += s_need[w];
+      s_base = tot ? atomicAdd(&g.counts[0], tot) : 0;
+    }
+    __syncthreads();
+    if (need && lane == 0) {
+      int at = s_base;
+      for (int w = 0; w < warp; w++) at += s_need[w];
+      g.slot[c] = at;
+      g.a_off[at] = ro;  // the whole oriented read (:708)
+      g.a_len[at] = rlen;
+      g.b_off[at] = boff;
+      g.b_len[at] = ov;
+    }
+    __syncthreads();  // s_need and s_base are rewritten next round
   }
-  if (same) {
-    g.slot[c] = -1;
-    return;
+  if (lane == 0) {
+    s_max[0][warp] = rmax;
+    s_max[1][warp] = omax;
+    s_max[2][warp] = nbad;
   }
-  const int at = atomicAdd(&g.counts[0], 1);
-  g.slot[c] = at;
-  g.a_off[at] = ro;  // the whole oriented read (:708)
-  g.a_len[at] = rlen;
-  g.b_off[at] = g.coff[id] + cstart;
-  g.b_len[at] = ov;
-  atomicMax(&g.counts[1], rlen);
-  atomicMax(&g.counts[2], ov);
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    int m = 0;
+    for (int w = 0; w < kPrepWarps; w++) m = max(m, s_max[threadIdx.x][w]);
+    if (threadIdx.x == 2) {
+      if (m) atomicAdd(&g.counts[3], 1);
+    } else if (m) {
+      atomicMax(&g.counts[1 + threadIdx.x], m);
+    }
+  }
 }
 
 struct FArgs {
@@ -331,7 +388,10 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
   if (!e) {
     g = KArgs{read, roff, rlen, cid, pic, pir, strand, n, K, cg->raw, cg->off, cg->len, ori, wstart, rstart0, ov,
               orient, slot, a_off, b_off, a_len, b_len, counts};
-    k_klign_prepare<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(g);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cg->device);
+    const int64_t blocks = std::min<int64_t>((n + kPrepWarps - 1) / kPrepWarps, (int64_t)sms * 8);
+    k_klign_prepare<<<(unsigned)blocks, kPrepWarps * 32, 0, st>>>(g);
     e = cudaGetLastError();
   }
   if (!e) e = cudaMemcpyAsync(h_counts, counts, sizeof(h_counts), cudaMemcpyDeviceToHost, st);
