@@ -124,6 +124,15 @@ def test_klign_caller_boundary_seeds_and_iupac(contigs, resident):
     assert np.array_equal(got["mismatches"], want["mismatches"])
 
 
+def test_klign_caller_arena_grows_and_is_reused(contigs, resident):
+    """One handle, batches of growing then shrinking size: the call arena kept on the handle
+    grows for the larger batch and is reused by the smaller ones."""
+    d = _driver()
+    for n, seed in ((500, 41), (40000, 42), (500, 43), (3, 44)):
+        cand = generate_candidates(contigs, n, seed=seed)
+        assert not _diff(klign_align(d, resident, cand), _want(contigs, cand, (1, 3, 5, 2, 2), False)), n
+
+
 def test_klign_caller_rejects_bad_candidates(contigs, resident):
     d = _driver()
     cand = generate_candidates(contigs, 10, seed=5)

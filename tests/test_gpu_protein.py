@@ -64,6 +64,15 @@ def test_protein_matches_oracle(built, lo, hi, n):
         assert not _diff(_driver(go, ge).align_protein(pairs, MAT, ENC), want), (go, ge)
 
 
+def test_protein_call_arena_grows_and_is_reused(built):
+    """One handle, batches of growing then shrinking size: the call arena kept on the handle
+    grows for the larger batch and is reused by the smaller ones."""
+    d = _driver()
+    for n, hi in ((50, 120), (3000, 500), (50, 120), (7, 60)):
+        pairs = _proteins(n, n + hi, 20, hi)
+        assert not _diff(d.align_protein(pairs, MAT, ENC), oracle.protein_batch(pairs, MAT, ENC, 11, 1)), n
+
+
 def test_protein_device_resident_batch(built):
     torch = pytest.importorskip("torch")
     from mhm2_staging_gb300.driver import DevicePairs
