@@ -81,6 +81,7 @@ constexpr int kInt16Ceiling = mhsw::V16::kBig - 1 - 64;  // leaves room for one 
 
 struct mhsw_driver {
   std::mutex mu;
+  std::mutex call_mu;  // calls on the call arena (caller side, protein), whole-call
   std::string err;
   bool inited = false;
   int device = 0;
@@ -1632,6 +1633,8 @@ int driver_device(mhsw_driver *d) { return d ? d->device : -1; }
 int driver_form(mhsw_driver *d) { return d ? d->form : MHSW_FORM_PLAIN; }
 bool driver_cigar(mhsw_driver *d) { return d && d->cigar; }
 const uint8_t *driver_a_codes(mhsw_driver *d) { return d ? d->a_code.p : nullptr; }
+
+std::mutex &driver_call_mutex(mhsw_driver *d) { return d->call_mu; }
 
 unsigned char *driver_call_arena(mhsw_driver *d, size_t bytes) {
   if (!d) return nullptr;

@@ -2,6 +2,7 @@
 // (not part of the C ABI).
 #pragma once
 #include <cstdint>
+#include <mutex>
 
 #include "../../include/mhsw.h"
 #include "mhsw_types.h"
@@ -37,6 +38,10 @@ void resident_timing(mhsw_driver *d);
 // entry point), kept on the handle between calls (grown when a batch needs more, never
 // shrunk); nullptr when the allocation fails.  Its contents are only valid during one call.
 unsigned char *driver_call_arena(mhsw_driver *d, size_t bytes);
+// Held by a call that uses the call arena, for the whole call (taken before the handle's
+// own lock, which the resident-batch functions above take inside), so calls that share a
+// handle stay serialised.
+std::mutex &driver_call_mutex(mhsw_driver *d);
 // Lays arrays out back to back at 256-byte boundaries: with base == nullptr it only sums
 // their sizes (off), otherwise it also hands out the pointers.
 struct Carve {

@@ -317,6 +317,7 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
     rbytes = std::max<int64_t>(rbytes, cand->read_off[i] + rl);
   }
   if (rbytes > INT32_MAX) return MHSW_ERR_LIMIT;
+  std::lock_guard<std::mutex> call_lk(mhsw::driver_call_mutex(d));
   cudaStream_t st = static_cast<cudaStream_t>(mhsw::driver_stream(d));
   cudaSetDevice(cg->device);
   KArgs g{};

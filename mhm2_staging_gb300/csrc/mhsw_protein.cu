@@ -229,6 +229,7 @@ int mhsw_align_protein(mhsw_driver *d, const mhsw_pairs *pairs, const int16_t *s
   if (dev < 0) return MHSW_ERR_STATE;
   for (int k = 0; k < kEnc; k++)
     if (encoding[k] < 0 || encoding[k] >= kAA) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> call_lk(mhsw::driver_call_mutex(d));
   cudaSetDevice(dev);
   cudaStream_t st = static_cast<cudaStream_t>(mhsw::driver_stream(d));
   int gO = 0, gE = 0;

@@ -133,6 +133,33 @@ def test_klign_caller_arena_grows_and_is_reused(contigs, resident):
         assert not _diff(klign_align(d, resident, cand), _want(contigs, cand, (1, 3, 5, 2, 2), False)), n
 
 
+def test_klign_caller_two_threads_share_a_handle(contigs, resident):
+    """Calls on one handle from two host threads (ctypes releases the GIL during the call)
+    are serialised by the handle: each thread gets its own batch's results."""
+    import threading
+
+    d = _driver()
+    batches = [generate_candidates(contigs, n, seed=s) for n, s in ((20000, 51), (5000, 52))]
+    wants = [_want(contigs, c, (1, 3, 5, 2, 2), False) for c in batches]
+    errors = []
+
+    def run(i):
+        try:
+            for _ in range(3):
+                msg = _diff(klign_align(d, resident, batches[i]), wants[i])
+                if msg:
+                    errors.append((i, msg))
+        except Exception as exc:  # reported below
+            errors.append((i, repr(exc)))
+
+    th = [threading.Thread(target=run, args=(i,)) for i in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+
+
 def test_klign_caller_rejects_bad_candidates(contigs, resident):
     d = _driver()
     cand = generate_candidates(contigs, 10, seed=5)
