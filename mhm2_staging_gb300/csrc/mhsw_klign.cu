@@ -389,9 +389,10 @@ int mhsw_klign_align(mhsw_driver *d, const mhsw_contigs *cg, const mhsw_candidat
   if (!e) {
     g = KArgs{read, roff, rlen, cid, pic, pir, strand, n, K, cg->raw, cg->off, cg->len, ori, wstart, rstart0, ov,
               orient, slot, a_off, b_off, a_len, b_len, counts};
-    int sms = 152;
+    int sms = 152, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cg->device);
-    const int64_t blocks = std::min<int64_t>((n + kPrepWarps - 1) / kPrepWarps, (int64_t)sms * 8);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_klign_prepare, kPrepWarps * 32, 0);
+    const int64_t blocks = std::min<int64_t>((n + kPrepWarps - 1) / kPrepWarps, (int64_t)sms * std::max(per_sm, 1));
     k_klign_prepare<<<(unsigned)blocks, kPrepWarps * 32, 0, st>>>(g);
     e = cudaGetLastError();
   }
