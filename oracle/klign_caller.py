@@ -1,5 +1,5 @@
 """CPU restatement of klign's caller side around the aligner (test infrastructure only:
-used by tests/ and bench.py's CPU-baseline leg as the checker, never by the product).
+used by tests/ and bench.py's CPU-baseline leg to check results and as the timed CPU baseline, never by the product).
 
 For each seed-hit candidate (read, contig, seed positions, strands), as
 src/klign.cpp does it:

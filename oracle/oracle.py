@@ -1,7 +1,7 @@
 """Loader for the CPU oracles -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use this module,
-as the checker.  The product path (libmhsw.so and mhm2_staging_gb300) never imports it.
+to check results and as the timed CPU baseline.  The product path (libmhsw.so and mhm2_staging_gb300) never imports it.
 
   liboracle.so   C restatement of the reference SSW result contract (sw_oracle.c);
                  pinned against the reference's own SSW and test/ssw-test.cpp's

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product path links or calls this
  * file: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
- * use it, as the checker.  Parity pinned against the reference's own SSW
+ * use it, to check results and as the timed CPU baseline.  Parity pinned against the reference's own SSW
  * (src/ssw/ssw.cpp + src/ssw/ssw_core.cpp, compiled from the reference
  * sources by oracle/Makefile into oracle/_ref/) and against the known-answer
  * cases of test/ssw-test.cpp:151-238 (fixtures in tests/golden/).
