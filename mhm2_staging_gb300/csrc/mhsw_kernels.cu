@@ -7,7 +7,8 @@
 //            prefixes A[0..a_end], B[0..b_end] (the reference's reverse pass,
 //            src/ssw/ssw_core.cpp:1166-1178 and src/adept-sw/kernel.cpp:335-509).
 //            Exact: every cell holding the score lies on an alignment from the end
-//            cell whose total gap length g obeys g*min(gO,gE) <= D*match - score with
+//            cell whose total gap length g obeys
+//            g*min(gO,gE) + max(gO-gE, 0) <= D*match - score with
 //            D <= min(a_end+1, b_end+1) diagonal steps,
 //            so the band |j - i| <= g contains it and banding only lowers other cells.
 //            k_rev_wave runs the wavefront engine on the reversed box for the rare
@@ -188,13 +189,22 @@ __host__ __device__ __forceinline__ int band_first_cap(int S, int mt, int M2) {
   return (int)(tt < M2 ? tt : M2);
 }
 
-// Total gap length any alignment reaching the score within the first t rows can have:
-// its diagonal steps D <= min(t, N2), so gaps <= (D * match - S) / min(gO, gE).
-// (D <= 65000 and match <= 127 keep the product inside 32 bits.)
-__host__ __device__ __forceinline__ int band_gap_bound(int t, int N2, int S, const Scoring &sc) {
+// Total gap length g (inserted plus deleted cells) of an alignment that scores S with at
+// most dmax diagonal steps.  Each diagonal step scores at most match, and g gap cells in
+// r >= 1 runs cost r*gO + (g - r)*gE >= g*min(gO, gE) + max(gO - gE, 0), so
+// g*min(gO, gE) + max(gO - gE, 0) <= dmax*match - S (g = 0 when that leaves no room for
+// one gap cell).  (dmax <= 65000 and match <= 127 keep the product inside 32 bits.)
+__host__ __device__ __forceinline__ int gap_cells_bound(int dmax, int S, const Scoring &sc) {
   const int gmin = sc.gap_open < sc.gap_extend ? sc.gap_open : sc.gap_extend;
-  const int dmax = t < N2 ? t : N2;
-  return (dmax * sc.match - S) / (gmin > 0 ? gmin : 1);
+  const int g1 = gmin > 0 ? gmin : 1;
+  const int slack = dmax * sc.match - S - (sc.gap_open > sc.gap_extend ? sc.gap_open - sc.gap_extend : 0);
+  return slack < g1 ? 0 : slack / g1;
+}
+
+// Total gap length any alignment reaching the score within the first t rows can have:
+// its diagonal steps D <= min(t, N2).
+__host__ __device__ __forceinline__ int band_gap_bound(int t, int N2, int S, const Scoring &sc) {
+  return gap_cells_bound(t < N2 ? t : N2, S, sc);
 }
 
 // Band class of pair p (0 .. kBandClasses-1), kBandClasses for the wavefront, or -1 when
@@ -300,13 +310,12 @@ __global__ void __launch_bounds__(256) k_rev_scatter(ResultSet rs, Scoring sc, c
   }
 }
 
-// One band row: W cells, dependency chain along the row through F.  Gap values are kept
-// biased by +gO (E^ = E + gO, F^ = F + gO) so H feeds their updates directly.  cb[u + d]
-// holds the code of band cell d's column OR 0x7770 (a byte_perm selector: byte 0 picks
-// the row's score for that code, bytes 1-3 read zero); columns outside [0, N2) carry the
-// PAD code, which scores -128: cells left of column 0 then stay exactly at the boundary
-// values and cells right of the last column stay below the score, so the band needs no
-// per-cell bound checks.
+// Band cells, two rows at a time.  Gap values are kept biased by +gO (E^ = E + gO,
+// F^ = F + gO) so H feeds their updates directly.  cb[u + d] holds the code of band cell
+// d's column OR 0x7770 (a byte_perm selector: byte 0 picks the row's score for that
+// code, bytes 1-3 read zero); columns outside [0, N2) carry the PAD code, which scores
+// -128: cells left of column 0 then stay exactly at the boundary values and cells right
+// of the last column stay below the score, so the band needs no per-cell bound checks.
 // BI: the table bytes already hold s + gO (every score >= -gO; PAD scores -gO), and
 // Hdiag + byte is a multiply-add by a runtime 1 (bias then carries that 1), which issues
 // on the FMA pipe instead of the integer ALU pipe the band saturates.  A PAD score of -gO
@@ -318,70 +327,59 @@ __device__ __forceinline__ int band_q(int hd, uint32_t byte, int bias) {
   else return hd + (int)byte + bias;
 }
 
+// Rows A (window offset u) and the row below it, B (offset u + 1), two cells behind.  B's
+// cell d reads A's cells d (diagonal) and d + 1 (above), written at the two steps before,
+// and overwrites A's cell d, which nothing needs any more; A's cell s reads only cells
+// >= s of the row above.  The two rows' dependency chains (F along each row) are
+// independent within a step, so they interleave.
+// Returns the largest cell key of the two rows, key = H * 128 + (64 for row A) + 63 - d
+// (W <= 63): its H is the larger row maximum, and among cells holding it the key picks
+// the upper row first, then its leftmost cell -- the first cell SSW's reverse scan meets
+// (rows = A positions before B positions).  The multiply-adds forming the keys issue on
+// the FMA pipe; one three-way max per step folds both rows' keys.
 template <int W, int NC, bool BI>
-__device__ __forceinline__ int band_row(const int (&cb)[NC], int u, uint32_t rp0, uint32_t rp1, int bias, int ngo,
-                                        int nge, int (&H)[W + 1], int (&E)[W + 1]) {
+__device__ __forceinline__ int band_pair(const int (&cb)[NC], int u, uint32_t ra0, uint32_t ra1, uint32_t rb0,
+                                         uint32_t rb1, int bias, int ngo, int nge, uint32_t k128, int (&H)[W + 1],
+                                         int (&E)[W + 1]) {
   constexpr int NEG = -(1 << 28);
-  int F = NEG;
-  int rm = 0;
-#pragma unroll
-  for (int d = 0; d < W; d++) {
-    const int q = band_q<BI>(H[d], __byte_perm(rp0, rp1, (uint32_t)cb[u + d]), bias);  // Hdiag + s + gO
-    const int e = __viaddmax_s32(E[d + 1], nge, H[d + 1]);
-    const int h = __viaddmax_s32_relu(__vimax3_s32(q, e, F), ngo, 0);
-    F = __viaddmax_s32(F, nge, h);
-    E[d] = e;
-    H[d] = h;
-    rm = max(rm, h);
-  }
-  return rm;
-}
-
-// Two band rows at once: row A (window offset u) and the row below it, B (offset u + 1),
-// two cells behind.  B's cell d reads A's cells d (diagonal) and d + 1 (above), written
-// at the two steps before, and overwrites A's cell d, which nothing needs any more; A's
-// cell s reads only cells >= s of the row above.  The two rows' dependency chains (F
-// along each row) are independent within a step, so they interleave; the arithmetic is
-// band_row's, cell for cell.  Returns the larger of the two rows' maxima.
-template <int W, int NC, bool BI>
-__device__ __forceinline__ int band_row2(const int (&cb)[NC], int u, uint32_t ra0, uint32_t ra1, uint32_t rb0,
-                                         uint32_t rb1, int bias, int ngo, int nge, int (&H)[W + 1], int (&E)[W + 1]) {
-  constexpr int NEG = -(1 << 28);
+  static_assert(W <= 63, "cell index must fit the key's six bits");
   int FA = NEG, FB = NEG;
-  int rm = 0;
+  int km = 0;
 #pragma unroll
   for (int s = 0; s < W + 2; s++) {
-    int ha = 0, hb = 0;
+    int ka = 0, kb = 0;
     if (s < W) {
       const int q = band_q<BI>(H[s], __byte_perm(ra0, ra1, (uint32_t)cb[u + s]), bias);
       const int e = __viaddmax_s32(E[s + 1], nge, H[s + 1]);
-      ha = __viaddmax_s32_relu(__vimax3_s32(q, e, FA), ngo, 0);
+      const int ha = __viaddmax_s32_relu(__vimax3_s32(q, e, FA), ngo, 0);
       FA = __viaddmax_s32(FA, nge, ha);
       E[s] = e;
       H[s] = ha;
+      ka = (int)mad_u32((uint32_t)ha, k128, (uint32_t)(64 + 63 - s));
     }
     if (s >= 2) {
       const int d = s - 2;
       const int q = band_q<BI>(H[d], __byte_perm(rb0, rb1, (uint32_t)cb[u + 1 + d]), bias);
       const int e = __viaddmax_s32(E[d + 1], nge, H[d + 1]);
-      hb = __viaddmax_s32_relu(__vimax3_s32(q, e, FB), ngo, 0);
+      const int hb = __viaddmax_s32_relu(__vimax3_s32(q, e, FB), ngo, 0);
       FB = __viaddmax_s32(FB, nge, hb);
       E[d] = e;
       H[d] = hb;
+      kb = (int)mad_u32((uint32_t)hb, k128, (uint32_t)(63 - d));
     }
-    rm = __vimax3_s32(rm, ha, hb);
+    km = __vimax3_s32(km, ka, kb);
   }
-  return rm;
+  return km;
 }
 
 // Pass 3 (one launch per class C): the banded search over the class's segment.  Rows go
-// in blocks of U; the band's codes live in a register window of W + U columns that
-// slides by U columns per block (one load per new column), and the row's scores come from
-// a per-block table indexed by the A code.  A row's maximum exceeds the largest maximum
-// of the rows before it by at most match (H <= Hdiag + match; E and F only lose), so
-// while that running maximum is below S - 2 * match neither of the next two rows can
-// reach S: those go two at a time (band_row2) with no search for the first cell; the
-// rows that may reach S go one at a time.
+// in pairs, in blocks of U; the band's codes live in a register window of W + U columns
+// that slides by U columns per block (one load per new column), and the rows' scores
+// come from a per-block table indexed by the A code.  No cell of the reversed box exceeds
+// the score, so the first cell reaching S in scan order is the largest key of the first
+// row pair whose key reaches S * 128: every thread runs the same row-pair code whether or
+// not its pair is about to reach the score.  A row past the box's last (an odd box) gets
+// the PAD row, whose cells stay below S, and its upper row wins every tie anyway.
 template <int WB, int C, bool BI>
 __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl) {
   constexpr int NEG = -(1 << 28);
@@ -390,13 +388,15 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
   constexpr int U = W <= 15 ? 8 : (W <= 31 ? 4 : 2);
   constexpr int NC = W + U;
   static_assert(G == band_half(C), "band class and width disagree");
-  // per A code 0..4: s(a, c) + off as bytes c = 0..3 | c = 4, PAD; off = gO (BI) or 128
+  static_assert(U % 2 == 0, "rows go in pairs within a block");
+  // per A code 0..4: s(a, c) + off as bytes c = 0..3 | c = 4, PAD; off = gO (BI) or 128;
+  // code 5 (PAD, rows past the box): every column scores -off
   __shared__ uint32_t rptab[2 * 8];
   const int toff = BI ? sc.gap_open : 128;
-  if (threadIdx.x < 5) {
+  if (threadIdx.x < 6) {
     const int a = threadIdx.x;
     uint32_t r0 = 0, r1 = 0;
-    for (int c = 0; c < 5; c++) {
+    for (int c = 0; c < 5 && a < kCodePad; c++) {
       const uint32_t v = (uint32_t)(sub_score(a, c, sc, 128) + toff) & 0xffu;
       if (c < 4) r0 |= v << (8 * c);
       else r1 = v;  // byte 1 (PAD) and above stay 0: score -off
@@ -406,8 +406,10 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
   }
   __syncthreads();
   const int mt = sc.match;
-  // BI: bias is a 1 the compiler cannot fold (gap_open is positive and below 2^30)
+  // BI: bias is a 1 the compiler cannot fold (gap_open is positive and below 2^30); k128
+  // likewise a 128, so the key multiply-adds stay on the FMA pipe
   const int bias = BI ? (sc.gap_open >> 30) + 1 : sc.gap_open - 128, ngo = -sc.gap_open, nge = -sc.gap_extend;
+  const uint32_t k128 = (uint32_t)(sc.gap_open >> 30) + 128u;
   int64_t off = 0;
 #pragma unroll
   for (int c = 0; c < C; c++) off += wl.band_counts[c];
@@ -436,45 +438,26 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
 #pragma unroll
     for (int k = 0; k < NC; k++) cb[k] = code_at(k - G);
     int i = 0;  // first row of the current block; the window covers columns i - G + [0, NC)
-    int rrun = 0;  // largest row maximum so far
     for (;;) {
       if (band_gap_bound(t, N2, S, sc) > G) {
         escalate = true;
         break;
       }
       while (i < t && !found) {
-        static_assert(U % 2 == 0, "rows go in pairs within a block");
+        // t is a multiple of U below M2, so a row pair starting below t ends below t
+        // unless t == M2 (its lower row is then the PAD row)
 #pragma unroll
         for (int u = 0; u < U; u += 2) {
           const int row = i + u;
           if (!found && row < t) {
-            if (row + 1 < t && rrun < S - 2 * mt) {
-              const int ca = a[-row], cc = a[-(row + 1)];
-              const int rm = band_row2<W, NC, BI>(cb, u, rptab[2 * ca], rptab[2 * ca + 1], rptab[2 * cc],
-                                              rptab[2 * cc + 1], bias, ngo, nge, H, E);
-              rrun = max(rrun, rm);
-            } else {
-#pragma unroll
-              for (int v = 0; v < 2; v++) {
-                const int r = row + v;
-                if (!found && r < t) {
-                  const int ca = a[-r];
-                  const int rm = band_row<W, NC, BI>(cb, u + v, rptab[2 * ca], rptab[2 * ca + 1], bias, ngo, nge, H, E);
-                  rrun = max(rrun, rm);
-                  if (rm >= S) {
-                    // first cell of this row that reaches the score
-#pragma unroll
-                    for (int d = 0; d < W; d++) {
-                      const int j = r - G + d;
-                      if (!found && j >= 0 && j < N2 && H[d] >= S) {
-                        found = true;
-                        fi = r;
-                        fj = j;
-                      }
-                    }
-                  }
-                }
-              }
+            const int ca = a[-row];
+            const int cc = row + 1 < M2 ? (int)a[-(row + 1)] : kCodePad;
+            const int km = band_pair<W, NC, BI>(cb, u, rptab[2 * ca], rptab[2 * ca + 1], rptab[2 * cc],
+                                                rptab[2 * cc + 1], bias, ngo, nge, k128, H, E);
+            if ((km >> 7) >= S) {
+              found = true;
+              fi = row + 1 - ((km >> 6) & 1);
+              fj = fi - G + (63 - (km & 63));
             }
           }
         }
@@ -490,7 +473,7 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
     }
     append_agg(wl.wide, wl.wide_count, wl.cap, p, escalate);
     if (escalate) continue;
-    if (!found) {
+    if (!found || fi >= M2 || fj < 0 || fj >= N2) {
       rs.flag[p] |= kFlagTooLong;  // inconsistent; reported as an error by the driver
       rs.a_beg[p] = -1;
       rs.b_beg[p] = 0;
@@ -588,7 +571,6 @@ __global__ void __launch_bounds__(256) k_rev_wave(PairSet ps, ResultSet rs, Scor
   gs.pad = pad;
   gs.bcap = bcap;
   constexpr int RS = 2 * K * G;
-  const int gmin = sc.gap_open < sc.gap_extend ? sc.gap_open : sc.gap_extend;
   const int64_t total = *wl.wide_count < wl.cap ? *wl.wide_count : wl.cap;
   const int64_t gid = (int64_t)blockIdx.x * gpb + grp;
   const int64_t gstride = (int64_t)gridDim.x * gpb;
@@ -599,9 +581,8 @@ __global__ void __launch_bounds__(256) k_rev_wave(PairSet ps, ResultSet rs, Scor
     if (S < s_lo || S > s_hi) continue;
     const int ie = rs.a_end[p], je = rs.b_end[p];
     const int M2 = ie + 1;
-    const long long dmax = M2 < je + 1 ? M2 : je + 1;
-    long long gbl = (dmax * sc.match - S) / (gmin > 0 ? gmin : 1);
-    if (gbl < 0) gbl = 0;
+    const int dmax = M2 < je + 1 ? M2 : je + 1;
+    const long long gbl = gap_cells_bound(dmax, S, sc);
     long long n2 = (long long)M2 + gbl + 1;
     if (n2 > je + 1) n2 = je + 1;
     const int N2 = (int)n2;
