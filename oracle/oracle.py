@@ -6,8 +6,14 @@ to check results and as the timed CPU baseline.  The product path (libmhsw.so an
   liboracle.so   C restatement of the reference SSW result contract (sw_oracle.c);
                  pinned against the reference's own SSW and test/ssw-test.cpp's
                  known answers (tests/golden/).
-  libssw_ref.so  the reference SSW itself (src/ssw/ssw.cpp + ssw_core.cpp), compiled
-                 from the reference checkout by oracle/Makefile; x86_64 only.
+  libssw_ref.so  the reference SSW itself (src/ssw/ssw.cpp + ssw_core.cpp), compiled by
+                 oracle/Makefile: on x86_64 from the reference checkout with SSE2; on
+                 aarch64 from the unmodified sources staged in oracle/_ref/ssw_src/
+                 (git-ignored) through oracle/sse2_shim/ (NEON).
+  libssw_ref_shim.so  (x86_64) the same sources through the shim's portable vector form,
+                 checked bit for bit against the SSE2 build.
+
+The reference checkout is found through the MHSW_REFERENCE environment variable.
 """
 from __future__ import annotations
 
@@ -23,23 +29,32 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "liboracle.so"
 REF_SO = HERE / "_ref" / "libssw_ref.so"
+REF_SHIM_SO = HERE / "_ref" / "libssw_ref_shim.so"
+STAGED_SSW = HERE / "_ref" / "ssw_src"
 REFERENCE_ROOT = Path(os.environ.get("MHSW_REFERENCE", "/root/reference"))
 
 _P = C.c_void_p
 _ORACLE = None
-_REF = None
+_REF: dict = {}
 
 
 def build(with_reference: bool | None = None) -> None:
-    """Builds liboracle.so; where the reference checkout is present, also libssw_ref.so
-    (x86_64) and the ADEPT comparator cubin (any host with nvcc)."""
+    """Builds liboracle.so.  Where the reference checkout is present (the x86_64 build
+    container): libssw_ref.so (SSE2), its shim twin libssw_ref_shim.so, the staged copy of
+    the SSW sources for the aarch64 host, and the ADEPT comparator cubin.  On aarch64 with
+    the staged sources: libssw_ref.so through the NEON shim."""
     subprocess.run(["make", "-s", "-C", str(HERE), "_build/liboracle.so"], check=True)
     if with_reference is False:
         return
-    if (REFERENCE_ROOT / "src" / "ssw" / "ssw.cpp").exists() and platform.machine() == "x86_64":
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_ROOT}"], check=True)
+    ref = f"REF={REFERENCE_ROOT}"
+    if (REFERENCE_ROOT / "src" / "ssw" / "ssw.cpp").exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "stage", ref], check=True)
+        if platform.machine() == "x86_64":
+            subprocess.run(["make", "-s", "-C", str(HERE), "ref", "ref-shim", ref], check=True)
+    if platform.machine() != "x86_64" and (STAGED_SSW / "ssw_core.cpp").exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
     if (REFERENCE_ROOT / "src" / "adept-sw" / "kernel.cpp").exists() and shutil.which("nvcc"):
-        subprocess.run(["make", "-s", "-C", str(HERE), "adept", f"REF={REFERENCE_ROOT}"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), "adept", ref], check=True)
 
 
 def _bind(lib: C.CDLL, name: str) -> None:
@@ -79,12 +94,18 @@ def reference_available() -> bool:
     return REF_SO.exists()
 
 
-def ref_lib() -> C.CDLL:
-    global _REF
-    if _REF is None:
-        if not REF_SO.exists():
-            raise RuntimeError("reference SSW not built (oracle/_ref/libssw_ref.so)")
-        lib = C.CDLL(str(REF_SO))
+def reference_build_kind() -> str:
+    """How libssw_ref.so was built here: "sse2" (x86_64, the reference's own vector code)
+    or "sse2-shim-neon" (aarch64, through oracle/sse2_shim)."""
+    return "sse2" if platform.machine() == "x86_64" else "sse2-shim-neon"
+
+
+def ref_lib(path: Path | None = None) -> C.CDLL:
+    path = Path(path or REF_SO)
+    if path not in _REF:
+        if not path.exists():
+            raise RuntimeError(f"reference SSW not built ({path})")
+        lib = C.CDLL(str(path))
         _bind(lib, "ssw_ref_align_batch")
         _bind(lib, "ssw_ref_align_batch7")
         _bind_cigar(lib, "ssw_ref_cigar_batch")
@@ -94,8 +115,8 @@ def ref_lib() -> C.CDLL:
         lib.ssw_ref_align.restype = C.c_int
         lib.ssw_ref_align.argtypes = [C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_int, C.c_int, _P]
-        _REF = lib
-    return _REF
+        _REF[path] = lib
+    return _REF[path]
 
 
 def _run(lib, fn, pairs, scoring, threads, width=5):
@@ -127,12 +148,14 @@ def align_batch_lanes(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None
     return _run(oracle_lib(), "sw_oracle_align_batch_lanes", pairs, scoring, threads or (os.cpu_count() or 1))
 
 
-def ref_align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, score2: bool = False) -> np.ndarray:
+def ref_align_batch(pairs, scoring=(1, 3, 5, 2, 2), threads: int | None = None, score2: bool = False,
+                    lib: Path | None = None) -> np.ndarray:
     """The reference SSW, called as klign calls it (src/klign.cpp:257); n x 7 with
-    sw_score_next_best and ref_end_next_best when score2."""
+    sw_score_next_best and ref_end_next_best when score2.  lib selects another build of
+    it (REF_SHIM_SO)."""
     if score2:
-        return _run(ref_lib(), "ssw_ref_align_batch7", pairs, scoring, threads or (os.cpu_count() or 1), 7)
-    return _run(ref_lib(), "ssw_ref_align_batch", pairs, scoring, threads or (os.cpu_count() or 1))
+        return _run(ref_lib(lib), "ssw_ref_align_batch7", pairs, scoring, threads or (os.cpu_count() or 1), 7)
+    return _run(ref_lib(lib), "ssw_ref_align_batch", pairs, scoring, threads or (os.cpu_count() or 1))
 
 
 def _run_cigar(lib, fn, pairs, scoring, threads, ops_cap):

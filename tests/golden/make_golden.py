@@ -14,7 +14,13 @@ $MHSW_REFERENCE) on x86_64; the GPU machine needs only the committed JSON files.
   ssw_reference_samples.json
       Seeded sample pairs of the measured workloads and hand-made edge cases with the
       reference SSW's (score, a_begin, a_end, b_begin, b_end) under those four scorings.
-  Both files also record, per scoring, the reference's second-best score and its row
+  ssw_reference_config0.npz
+      The reference SSW's outputs (score, a_begin, a_end, b_begin, b_end,
+      sw_score_next_best, ref_end_next_best) for all 10,000 pairs of the 150/300 bp
+      workload (workloads.generate(0), regenerated from its seed where the fixture is
+      read) at scoring 1/3/5/2/2, from the x86_64 SSE2 build: the record other builds of
+      the reference (the aarch64 NEON-shim build) are checked against.
+  The two JSON files also record, per scoring, the reference's second-best score and its row
   ("reference_next_best": sw_score_next_best, ref_end_next_best) for maskLen =
   max(len(A)/2, 15) as klign passes it, and what the reference returns with
   report_cigar (Filter(true, true, 0, 32767), the filter klign's post-assembly alignment
@@ -210,5 +216,24 @@ def make_protein(oracle, Pairs) -> None:
     print(f"{len(a)} protein pairs")
 
 
+def make_config0(oracle) -> None:
+    import numpy as np
+
+    from mhm2_staging_gb300 import workloads
+
+    oracle.build(with_reference=True)
+    pairs = workloads.generate(0)
+    out = oracle.ref_align_batch(pairs, SCORINGS["measured"], score2=True)
+    np.savez_compressed(HERE / "ssw_reference_config0.npz", out=out.astype(np.int32),
+                        scoring=np.array(SCORINGS["measured"], dtype=np.int32))
+    print(f"config 0: {pairs.n} pairs")
+
+
 if __name__ == "__main__":
-    main()
+    from oracle import oracle as _oracle
+
+    if sys.argv[1:] == ["config0"]:
+        make_config0(_oracle)
+    else:
+        main()
+        make_config0(_oracle)

@@ -336,3 +336,51 @@ def test_protein_oracle_vs_live_reference():
     enc = oracle.protein_encoding()
     for go, ge in ((11, 1), (7, 3), (4, 1)):
         assert np.array_equal(oracle.protein_batch(pairs, m, enc, go, ge), oracle.ref_protein_batch(pairs, m, enc, go, ge))
+
+
+def _config0_record():
+    rec = np.load(GOLDEN / "ssw_reference_config0.npz")
+    return rec["out"], tuple(int(x) for x in rec["scoring"])
+
+
+def test_config0_record_vs_oracle():
+    """The recorded reference outputs of the 150/300 bp workload (all 10,000 pairs, score2
+    fields included) equal the oracle's."""
+    from mhm2_staging_gb300 import workloads
+
+    want, sc = _config0_record()
+    pairs = workloads.generate(0)
+    assert np.array_equal(oracle.align_batch(pairs, sc, score2=True), want)
+
+
+def test_sse2_shim_build_vs_sse2_build():
+    """The reference SSW compiled through oracle/sse2_shim (its portable vector form, on
+    this x86_64 host) gives what the genuine SSE2 build gives, on the 150/300 bp workload
+    and on samples of the others."""
+    from mhm2_staging_gb300 import workloads
+
+    if not (oracle.reference_available() and oracle.REF_SHIM_SO.exists()):
+        pytest.skip("needs the reference checkout on x86_64 (SSE2 build and its shim twin)")
+    want, sc = _config0_record()
+    assert np.array_equal(oracle.ref_align_batch(workloads.generate(0), sc, score2=True,
+                                                 lib=oracle.REF_SHIM_SO), want)
+    for cfg, n in ((1, 5000), (2, 5000), (4, 500)):
+        p = workloads.generate(cfg, n=n, first=7000)
+        assert np.array_equal(oracle.ref_align_batch(p, sc, score2=True, lib=oracle.REF_SHIM_SO),
+                              oracle.ref_align_batch(p, sc, score2=True)), cfg
+
+
+@pytest.mark.parametrize("host", ["build_container", pytest.param("gpu_host", marks=pytest.mark.gpu)])
+def test_reference_build_vs_x86_record(host):
+    """Whatever build of the reference SSW this host has -- SSE2 on x86_64, the NEON shim
+    on the GPU host's aarch64 -- reproduces the x86_64 SSE2 record of the 150/300 bp
+    workload bit for bit (the GPU-marked case runs where the GPU tests run, the host
+    that times the reference as the CPU baseline)."""
+    from mhm2_staging_gb300 import workloads
+
+    if not oracle.reference_available():
+        pytest.skip("reference SSW not built on this host")
+    want, sc = _config0_record()
+    got = oracle.ref_align_batch(workloads.generate(0), sc, score2=True)
+    bad = np.nonzero((got != want).any(axis=1))[0]
+    assert len(bad) == 0, f"{oracle.reference_build_kind()}: {len(bad)} pairs differ; first {bad[:5].tolist()}"
