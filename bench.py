@@ -11,8 +11,11 @@ synthetic pairs of the uneven-length workload (4,000,000 pairs: 60% 150 bp, 30% 
          results out, every step.
   plain  the plain drop-in kernel on the same pairs, for the batched-vs-plain ratio.
 
-Prints one JSON line on rank 0.  `--impl reference` times the CPU implementation of the
-path instead (the oracle port of the reference SSW, all host threads, bounded samples).
+Prints one JSON line on rank 0.  `--impl reference` times the reference's own CPU
+implementation of the path instead -- its SSW (src/ssw), compiled on this host (through an
+SSE2-to-NEON shim on aarch64) and called as klign calls it, one Aligner per host thread, on
+bounded samples of the workload -- with the oracle port beside it, and the reference's
+own CUDA kernels (ADEPT) on the same GPU.
 """
 from __future__ import annotations
 
@@ -92,30 +95,60 @@ class ClockSampler:
 
 
 CPU_PORT = ("the oracle's result contract vectorised across pairs (oracle/sw_lanes.cpp: 8 pairs per 128-bit "
-            "vector, 4 vectors interleaved on aarch64, portable GCC vectors; bit-exact with the scalar restatement; "
-            "on x86_64 it matches the reference SSE2 SSW's speed on the same pairs and threads)")
+            "vector, 4 vectors interleaved on aarch64, portable GCC vectors; bit-exact with the scalar restatement)")
 
 
-def cpu_baseline(pairs, budget_s: float = 12.0) -> dict:
-    """The oracle port (vectorised across pairs) timed on the host cores on a bounded
-    leading sample of the batch."""
+def _ref_implementation() -> str:
     from oracle import oracle
 
-    threads = os.cpu_count() or 1
+    how = ("with SSE2" if oracle.reference_build_kind() == "sse2" else
+           "through the SSE2-to-NEON shim oracle/sse2_shim (bit-exact with the x86_64 SSE2 build on the 150/300 bp "
+           "workload, tests/test_oracle.py)")
+    return ("the reference's own SSW (src/ssw/ssw.cpp + ssw_core.cpp, unmodified) compiled on this host " + how +
+            ", called as klign calls it (Aligner(1,3,5,2,2).Align(contig, read, len, Filter(true,false,0,32767), "
+            "&aln, max(len/2,15)), src/klign.cpp:257), one Aligner per thread, pairs handed out 64 at a time")
+
+
+def _cpu_engine():
+    """(kind, run(pairs, threads), description) of the CPU baseline: the reference SSW where
+    it is built on this host, else the oracle port."""
+    from oracle import oracle
+
+    if oracle.reference_available():
+        return "reference", (lambda p, t: oracle.ref_align_batch(p, SCORING, t)), _ref_implementation()
+    return "port", (lambda p, t: oracle.align_batch_lanes(p, SCORING, t)), CPU_PORT
+
+
+def _timed_sample(run, pairs, threads: int, budget_s: float):
+    """Times run() on the leading sample of pairs that takes about budget_s."""
     n_probe = min(pairs.n, 20000)
-    probe = pairs.slice(0, n_probe)
     t0 = time.perf_counter()
-    oracle.align_batch_lanes(probe, SCORING, threads)
+    run(pairs.slice(0, n_probe), threads)
     dt = max(time.perf_counter() - t0, 1e-3)
     n = int(min(pairs.n, max(n_probe, n_probe * budget_s / dt)))
     sample = pairs.slice(0, n)
     t0 = time.perf_counter()
-    oracle.align_batch_lanes(sample, SCORING, threads)
-    dt = time.perf_counter() - t0
-    cells = sample.cells()
-    return {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": "port",
-            "sample": f"first {n} pairs of the same workload ({cells:.3g} forward cells, {dt:.1f} s)",
-            "implementation": CPU_PORT, "alignments_per_s": n / dt}
+    run(sample, threads)
+    return n, sample.cells(), time.perf_counter() - t0
+
+
+def cpu_baseline(pairs, budget_s: float = 12.0) -> dict:
+    """The reference SSW (or, where it is not built, the oracle port) timed on all host
+    cores on a bounded leading sample of the batch; the port beside it."""
+    from oracle import oracle
+
+    threads = os.cpu_count() or 1
+    kind, run, impl = _cpu_engine()
+    n, cells, dt = _timed_sample(run, pairs, threads, budget_s)
+    out = {"value": cells / dt / 1e9, "unit": "GCUPS", "cores": threads, "kind": kind,
+           "sample": f"first {n} pairs of the same workload ({cells:.3g} forward cells, {dt:.1f} s)",
+           "implementation": impl, "alignments_per_s": n / dt}
+    if kind == "reference":
+        pn, pcells, pdt = _timed_sample(lambda p, t: oracle.align_batch_lanes(p, SCORING, t), pairs, threads,
+                                        budget_s / 2)
+        out["port"] = {"value": pcells / pdt / 1e9, "unit": "GCUPS", "cores": threads,
+                       "sample": f"first {pn} pairs ({pdt:.1f} s)", "implementation": CPU_PORT}
+    return out
 
 
 def _adept_gpu(args) -> dict | None:
@@ -131,7 +164,7 @@ def _adept_gpu(args) -> dict | None:
     from oracle import oracle
 
     n = args.pairs or workloads.CONFIG_PAIRS[args.config]
-    pairs = workloads.generate(args.config, n=n)
+    pairs = workloads.generate(args.config, n=n, gen_lib=oracle.GEN_SO)
     ad = adept.Adept(0)
     batch = ad.upload(pairs)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -160,56 +193,67 @@ def run_reference(args) -> None:
     from mhm2_staging_gb300 import workloads
     from oracle import oracle
 
-    oracle.build(with_reference=False)
+    oracle.build()  # liboracle.so, the generator; libssw_ref.so where its sources are here
     threads = os.cpu_count() or 1
     per_step = args.ref_pairs
-    pairs = workloads.generate(args.config, n=per_step * (args.steps + args.warmup), seed=args.config)
-    times, cells = [], []
-    for s in range(args.warmup + args.steps):
-        sub = pairs.slice(s * per_step, (s + 1) * per_step)
-        t0 = time.perf_counter()
-        oracle.align_batch_lanes(sub, SCORING, threads)
-        dt = time.perf_counter() - t0
-        if s >= args.warmup:
-            times.append(dt)
-            cells.append(sub.cells())
+    # inputs from the oracle's own build of the seeded generator (nothing of the product loaded)
+    pairs = workloads.generate(args.config, n=per_step * (args.steps + args.warmup), seed=args.config,
+                               gen_lib=oracle.GEN_SO)
+    kind, run, impl = _cpu_engine()
+
+    def timed(fn) -> tuple[list, list]:
+        times, cells = [], []
+        for s in range(args.warmup + args.steps):
+            sub = pairs.slice(s * per_step, (s + 1) * per_step)
+            t0 = time.perf_counter()
+            fn(sub, threads)
+            dt = time.perf_counter() - t0
+            if s >= args.warmup:
+                times.append(dt)
+                cells.append(sub.cells())
+        return times, cells
+
+    times, cells = timed(run)
     tot = sum(times)
     gcups = sum(cells) / tot / 1e9
+    sample = f"{per_step} pairs per step of the same workload, steps {args.warmup}.. of the seeded stream"
     line = {
         "impl": "reference", "metric": "GCUPS", "value": gcups, "unit": "GCUPS", "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "int16 (SSW's u8 then i16 saturating passes)"
+        if kind == "reference" else "int32", "data": "synthetic (seeded generator)",
         "config": {"workload": WORKLOAD_NAME, "pairs_per_step": per_step, "scoring": list(SCORING),
                    "cache": "inputs larger than L2 (CPU run)"},
         "alignments_per_s": per_step * args.steps / tot,
-        "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": threads, "kind": "port",
-                         "sample": f"{per_step} pairs per step of the same workload (the reference SSW has only "
-                                   f"SSE2 and AltiVec code and its sources do not ship to this host)",
-                         "implementation": CPU_PORT},
+        "cpu_baseline": {"value": gcups, "unit": "GCUPS", "cores": threads, "kind": kind, "sample": sample,
+                         "implementation": impl},
         "e2e": {"value": gcups, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if kind == "reference":
+        pt, pc = timed(lambda p, t: oracle.align_batch_lanes(p, SCORING, t))
+        line["port"] = {"value": sum(pc) / sum(pt) / 1e9, "unit": "GCUPS", "cores": threads, "sample": sample,
+                        "implementation": CPU_PORT}
     ad = _adept_gpu(args)
     if ad is not None:
         line["adept_gpu"] = ad
     print(json.dumps(line), flush=True)
 
 
-def run_serving(args) -> None:
+SERVING_WORKLOAD = ("serving: 200 MB resident contigs (lognormal(ln 2000, 1.0) in [200, 200000]), request batches "
+                    "log-uniform in [1k, 64k], reads U[100,250] bp, window read +-200 bp")
+
+
+def serving_measure(batches_per_level: int, slots: int, pool_n: int) -> dict:
     """Serving workload: 200 MB of resident contigs; request batches (sizes log-uniform in
     [1k, 64k] requests, reads U[100,250] bp from the contigs, 2% divergence) aligned against
     their seed-hit windows (read +-200 bp).  First the saturated throughput (every batch
     submitted at once), then open-loop Poisson arrivals at 25/50/90% of it, with the
     latency percentiles of the batches (submission to completion)."""
-    ws, rank, _ = _dist()
-    if rank != 0:
-        return
-    from mhm2_staging_gb300 import build as mbuild
     from mhm2_staging_gb300 import serving as S
 
-    mbuild.build()
     rng = np.random.default_rng(3)
     contigs = S.generate_contigs(200 << 20, seed=3)
-    pool = S.generate_requests(contigs, args.serving_pool, seed=3)
+    pool = S.generate_requests(contigs, pool_n, seed=3)
 
     def batches(count: int):
         out, at = [], 0
@@ -221,14 +265,14 @@ def run_serving(args) -> None:
             at += k
         return out
 
-    srv = S.Server(slots=args.slots, max_pairs_per_batch=65536)
+    srv = S.Server(slots=slots, max_pairs_per_batch=65536)
     srv.load_contigs(contigs)
     clk = ClockSampler(0)
-    # warm-up (slot set-up and autotuning on real batches)
-    for t in [srv.submit(b) for b in batches(3 * args.slots)]:
+    # warm-up (slot set-up and tuning on real batches)
+    for t in [srv.submit(b) for b in batches(3 * slots)]:
         srv.wait(t)
     # saturated throughput
-    sat = batches(args.serving_batches)
+    sat = batches(batches_per_level)
     clk.start()
     t0 = time.perf_counter()
     ts = [srv.submit(b) for b in sat]
@@ -241,7 +285,7 @@ def run_serving(args) -> None:
     mean_batch = sat_pairs / len(sat)
     loads = []
     for frac in (0.25, 0.5, 0.9):
-        bl = batches(args.serving_batches)
+        bl = batches(batches_per_level)
         r = S.run_open_loop(srv, bl, rate_hz=frac * peak / mean_batch, seed=int(frac * 100))
         r["load"] = frac
         r["offered_pairs_per_s"] = frac * peak
@@ -249,17 +293,30 @@ def run_serving(args) -> None:
     clocks = clk.stop()
     st = srv.stats()
     srv.close()
+    return {"workload": SERVING_WORKLOAD, "slots": slots, "max_pairs_per_batch": 65536,
+            "batches_per_level": batches_per_level,
+            "saturated": {"pairs_per_s": peak, "gcups": sat_cells / wall / 1e9, "batches": len(sat), "wall_s": wall},
+            "loads": loads, "server": st, "clocks": clocks}
+
+
+def run_serving(args) -> None:
+    """The serving workload alone (serving_measure), as its own JSON line: the headline is
+    the p99 batch latency at 90% of the saturated load."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from mhm2_staging_gb300 import build as mbuild
+
+    mbuild.build()
+    m = serving_measure(args.serving_batches, args.slots, args.serving_pool)
     line = {
-        "metric": "p99 batch latency at 90% of saturated load", "value": loads[-1]["p99_ms"], "unit": "ms",
+        "metric": "p99 batch latency at 90% of saturated load", "value": m["loads"][-1]["p99_ms"], "unit": "ms",
         "n_gpus": 1, "steps": args.serving_batches, "warmup": 3 * args.slots, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "int16x2 (int32 re-run on overflow)",
         "data": "synthetic (seeded contigs and seed-hit requests)",
-        "config": {"workload": "serving: 200 MB resident contigs (lognormal(ln 2000, 1.0) in [200, 200000]), "
-                               "request batches log-uniform in [1k, 64k], reads U[100,250] bp, window read +-200 bp",
-                   "slots": args.slots, "max_pairs_per_batch": 65536, "scoring": list(SCORING),
-                   "form": "batched persistent per micro-batch"},
-        "saturated": {"pairs_per_s": peak, "gcups": sat_cells / wall / 1e9, "batches": len(sat), "wall_s": wall},
-        "loads": loads, "server": st, "clocks": clocks,
+        "config": {"workload": SERVING_WORKLOAD, "slots": args.slots, "max_pairs_per_batch": 65536,
+                   "scoring": list(SCORING), "form": "batched persistent per micro-batch"},
+        "saturated": m["saturated"], "loads": m["loads"], "server": m["server"], "clocks": m["clocks"],
     }
     print(json.dumps(line), flush=True)
 
@@ -279,6 +336,7 @@ def run_paths(drv, dev, torch, stream) -> dict:
     specs = [("150bp_vs_300bp_10k_pairs_plain", 0, 10_000, FORM_PLAIN, None),
              ("150bp_vs_300bp_10k_pairs_batched", 0, 10_000, FORM_BATCHED, None),
              ("reads_100_250bp_1M_pairs_30pct_unrelated", 1, 1_000_000, FORM_BATCHED, None),
+             ("reads_100_250bp_1M_pairs_30pct_unrelated_plain", 1, 1_000_000, FORM_PLAIN, None),
              ("250bp_vs_2_8kb_refs_200k_pairs", 4, 200_000, FORM_BATCHED, None),
              ("uneven_200k_pairs_all_int32", 2, 200_000, FORM_BATCHED, 0),
              ("uneven_200k_pairs_score2_mode", 2, 200_000, FORM_BATCHED, "score2"),
@@ -328,6 +386,31 @@ def run_paths(drv, dev, torch, stream) -> dict:
     out["klign_caller_200k_candidates"] = _klign_caller_path(drv)
     out["protein_100k_pairs_100_500aa"] = _protein_path()
     out["uneven_1M_pairs_in_20k_pair_calls_host"] = _block_calls_path(drv)
+    out["uneven_1M_pairs_cpp_dropin_20k_blocks"] = _cpp_dropin_path()
+    return out
+
+
+def _cpp_dropin_path(n: int = 1_000_000, per_block: int = 20_000, passes: int = 3) -> dict:
+    """klign's GPU call sequence through the C++ drop-in header (klign_block_bench): the
+    uneven workload's first 1M pairs as 20,000-pair std::vector<std::string> blocks,
+    run_kernel_forwards -> kernel_block -> run_kernel_backwards -> kernel_block ->
+    get_aln_results per block (src/klign.cpp:356-388), in its own process on its own
+    handle; the plain drop-in form (as klign calls it) and the batched form."""
+    import tempfile
+
+    from mhm2_staging_gb300 import build as mbuild
+    from mhm2_staging_gb300 import workloads
+
+    pp = workloads.generate(2, n=n)
+    out = {"interface": "include/adept-sw/driver.hpp (C++ header over the C ABI), klign's call sequence"}
+    with tempfile.TemporaryDirectory() as td:
+        f = Path(td) / "pairs.bin"
+        pp.write_file(f)
+        for form in ("plain", "batched"):
+            r = subprocess.run([str(mbuild.block_bench_path()), str(f), str(per_block), str(passes), form],
+                               capture_output=True, text=True, timeout=600)
+            out[form] = (json.loads(r.stdout.strip().splitlines()[-1]) if r.returncode == 0 else
+                         {"error": (r.stdout + r.stderr)[-400:]})
     return out
 
 
@@ -473,6 +556,30 @@ def _cigar_cpu_port(pairs, n: int = 20_000) -> dict:
             "sample": f"first {sub.n} pairs of the slice ({dt:.1f} s)"}
 
 
+def _call_breakdown(recs: list[dict]) -> dict:
+    """Per-call device phases of pipelined host-batch calls (mhsw_call_history), ms: each
+    call's copies in, the GPU's idle time before its kernels (after the previous call's
+    kernels ended), its kernels, and its result copy out.  A call's kernels start when both
+    its copies in have ended and the stream is free."""
+    out = {"copy_in_ms": [], "kernels_ms": [], "idle_before_kernels_ms": [], "copy_out_ms": [],
+           "kernels_waited_for_copies": 0}
+    prev_end = None
+    for r in recs:
+        start = max(r["stream_ready"], r["copy_in_end"]) if r["copy_in_end"] >= 0 else r["stream_ready"]
+        out["copy_in_ms"].append(round(r["copy_in_end"] - r["copy_in_start"], 3) if r["copy_in_end"] >= 0 else None)
+        out["kernels_ms"].append(round(r["begin_done"] - start, 3))
+        out["copy_out_ms"].append(round(r["done"] - r["begin_done"], 3))
+        if prev_end is not None:
+            out["idle_before_kernels_ms"].append(round(max(0.0, start - prev_end), 3))
+            if r["copy_in_end"] > r["stream_ready"]:
+                out["kernels_waited_for_copies"] += 1
+        prev_end = r["done"]
+    if recs:
+        out["span_ms"] = round(recs[-1]["done"] - (recs[0]["copy_in_start"] if recs[0]["copy_in_start"] >= 0
+                                                    else recs[0]["stream_ready"]), 3)
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -488,12 +595,15 @@ def main() -> None:
     ap.add_argument("--no-paths", action="store_true", help="skip the per-workload path measurements")
     ap.add_argument("--cigar", action="store_true",
                     help="CIGAR mode in the timed regions (SSW's report_cigar output as well; e2e copies it back)")
-    ap.add_argument("--workload", choices=["batch", "serving", "protein"], default="batch",
+    ap.add_argument("--workload", choices=["batch", "serving", "protein", "klign"], default="batch",
                     help="batch: the uneven-length batch (default); serving: latency under offered load; "
                          "protein: the protein path alone (--pairs pairs, default 100000)")
     ap.add_argument("--slots", type=int, default=3, help="serving: micro-batches in flight")
     ap.add_argument("--serving-batches", type=int, default=400, help="serving: request batches per load level")
     ap.add_argument("--serving-pool", type=int, default=2_000_000, help="serving: distinct requests generated")
+    ap.add_argument("--serving-batches-default", type=int, default=200,
+                    help="serving leg of the default run: request batches per load level")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving leg of the default run")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -501,6 +611,15 @@ def main() -> None:
         return run_serving(args)
     if args.workload == "protein":
         print(json.dumps({"workload": "protein", **_protein_path(args.pairs or 100_000)}), flush=True)
+        return None
+    if args.workload == "klign":
+        from mhm2_staging_gb300 import GPUDriver
+
+        kd = GPUDriver()
+        kd.init(0, 1, SCORING[0], -SCORING[1], -SCORING[2], -SCORING[3], 0)
+        kd.set_ambiguity(-SCORING[4])
+        print(json.dumps({"workload": "klign caller side, 200k candidates vs 64 MB contigs",
+                          **_klign_caller_path(kd, args.pairs or 200_000)}), flush=True)
         return None
 
     ws, rank, local = _dist()
@@ -555,9 +674,18 @@ def main() -> None:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
         return float(t.item())
 
-    # ---- warm-up (includes the batched form's one-time launch-shape tuning) ----------
-    for _ in range(max(args.warmup, 3)):
+    # ---- warm-up (the first call tunes the batched form on a sample of the batch) -----
+    tuning = None
+    for i in range(max(args.warmup, 3)):
+        w0 = time.perf_counter()
         drv.align_pairs_device(dp, out_dev.data_ptr(), form=FORM_BATCHED)
+        torch.cuda.synchronize(dev)
+        if i == 0:
+            tuning = drv.last_tuning()
+            tuning["first_call_wall_ms"] = (time.perf_counter() - w0) * 1e3
+    tuning["rows_per_lane"] = ("8-lane groups: 2K rows per lane with K = 4/6/8/10 for A up to 64/96/128/160 rows; "
+                               "16-lane groups: K = 6/8 for A up to 192/256 rows, 256-row strips beyond; A above "
+                               "lane_rows goes to 16-lane groups")
 
     # ---- timed region: device-resident batched form ----------------------------------
     clocks = ClockSampler(local)
@@ -624,11 +752,11 @@ def main() -> None:
     d2h = int(hout.nbytes)
     hp.extents()  # the batch's extents, known to the caller (as klign knows its longest read/contig)
     # Steps go through the async halves of the batch call (mhsw_align_pairs_async, then
-    # mhsw_align_wait once at the end): the handle keeps two calls in flight on two input
-    # sets, so step k + 1's copies in run while step k's kernels do.  Every step still
+    # mhsw_align_wait once at the end): the handle keeps three calls in flight on three
+    # input sets, so later steps' copies in run while step k's kernels do.  Every step still
     # copies its inputs from pinned host memory and its results back inside the timed
     # region.  The one-call-at-a-time figure is reported beside it as e2e_sequential.
-    houts = [hout, pinned(np.zeros((pairs.n, 5), dtype=np.int32))]
+    houts = [hout, pinned(np.zeros((pairs.n, 5), dtype=np.int32)), pinned(np.zeros((pairs.n, 5), dtype=np.int32))]
     for o in houts:
         drv.align_pairs(hp, form=FORM_BATCHED, out=o, hints=True)  # warm (sizes both input sets)
     # this host's copy rate: one plain pinned host -> device copy of the step's read bytes,
@@ -652,11 +780,12 @@ def main() -> None:
     t0 = time.perf_counter()
     cg = None
     for k in range(args.e2e_steps):
-        drv.align_pairs_async(hp, form=FORM_BATCHED, out=houts[k % 2], hints=True)
+        drv.align_pairs_async(hp, form=FORM_BATCHED, out=houts[k % 3], hints=True)
         if args.cigar:
             cg = drv.last_cigar(pairs.n)  # CIGAR mode completes each call before the next
     drv.wait()
     e2e_s = allmax((time.perf_counter() - t0) / args.e2e_steps)
+    e2e_calls = _call_breakdown(drv.call_history(args.e2e_steps))
     if args.cigar:
         d2h += int(cg.nops.nbytes + cg.mismatches.nbytes + cg.op_off.nbytes + cg.ops.nbytes)
     e2e_gcups = cells_all / e2e_s / 1e9
@@ -717,6 +846,13 @@ def main() -> None:
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(pairs)
 
+    # ---- serving (200 MB resident contigs), bounded: saturated, then 25/50/90% load ----
+    serving = None
+    if rank == 0 and ws == 1 and not args.no_serving:
+        del tens, out_dev
+        torch.cuda.empty_cache()
+        serving = serving_measure(args.serving_batches_default, args.slots, 1_000_000)
+
     if rank == 0:
         line = {
             "metric": "GCUPS", "value": gcups, "unit": "GCUPS", "n_gpus": ws, "steps": args.steps,
@@ -734,7 +870,8 @@ def main() -> None:
             "e2e": {"value": e2e_gcups, "unit": "GCUPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "host_to_device_gbs": h2d_gbs,
                     "ms_per_step": e2e_s * 1e3, "steps": args.e2e_steps,
-                    "mode": "async calls, two in flight: step k+1's copies overlap step k's kernels"},
+                    "mode": "async calls, three in flight: later steps' copies overlap step k's kernels",
+                    "calls": e2e_calls},
             "e2e_sequential": {"value": cells_all / e2e_seq_s / 1e9, "unit": "GCUPS", "ms_per_step": e2e_seq_s * 1e3,
                                "device_ms": seq_t["total_ms"], "fwd_ms": seq_t["fwd_ms"], "rev_ms": seq_t["rev_ms"],
                                "call_wall_ms": seq_wall, "call_device_ms": seq_dev,
@@ -743,8 +880,9 @@ def main() -> None:
                                        "of ms_per_step is host time); call_* = each call's wall time and "
                                        "device span"},
             "gpu_launches": launches,
+            "tuning": tuning,
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "paths": paths,
+            "paths": paths, "serving": serving,
             "overflow16_pairs": int(last["n_overflow16"]), "rev_wavefront_pairs": int(last["n_rev_wide"]),
         }
         print(json.dumps(line), flush=True)

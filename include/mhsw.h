@@ -16,7 +16,11 @@
  *     sw_sse2_byte, src/ssw/ssw_core.cpp:296) and "B" the one it profiles (its query).
  *     klign calls Align(contig, read, ...) (src/klign.cpp:257), so in klign's
  *     orientation A = read and B = contig window.  Tie-breaks follow SSW's roles.
- *   - A handle serialises its own calls; use one handle per host thread.
+ *   - A handle serialises its own calls; use one handle per host thread.  Calls that
+ *     keep device state on the handle between their own steps (mhsw_klign_align and the
+ *     protein entry point) also hold the handle for their whole call, so two threads may
+ *     share a handle for those; mixing them on a shared handle with the batch calls
+ *     (mhsw_align_pairs and its result readers) is not supported.
  *   - Result arrays returned by mhsw_get_aln_results() are owned by the handle and stay
  *     valid until the next mhsw_run_kernel_* call or mhsw_driver_destroy().
  */
@@ -88,6 +92,43 @@ typedef struct {
   int64_t n_cigar_generic;  /* CIGAR mode: pairs whose band or box exceeded the register
                              * kernels and took the generic kernel */
 } mhsw_timing;
+
+/* The batched form's tuning (no counterpart in the reference, whose launch shape follows
+ * the batch's longest sequences, src/adept-sw/driver.cpp:343-368): the configuration the
+ * handle's persistent forward kernels run with, and what its last tuning cost.  A batched
+ * call whose length signature (the A-length mix over the kernels' row classes, sampled
+ * where the host sees the lengths, and the classes of the longest A and B and of the
+ * batch size) moved away from the one the handle last tuned for re-tunes on a strided
+ * sample of at most 256k pairs of its batch before aligning it. */
+typedef struct {
+  int32_t threads_per_block;  /* persistent kernels' block size */
+  int32_t blocks_per_sm;      /* 0 = the occupancy limit */
+  int32_t lane_rows;          /* longest A (rows) aligned by 8-lane groups; longer A by 16-lane groups */
+  int32_t wide_try16;         /* 1: pairs whose score bound exceeds the int16 keys run int16 first */
+  int32_t last_call_tuned;    /* 1 when the last batched call ran the tuner */
+  int32_t trials;             /* timed trials of the last tuning */
+  int64_t sample_pairs;       /* pairs the last tuning's trials ran on */
+  int64_t tunings;            /* tunings by this handle so far */
+  double tune_wall_ms;        /* host wall time the last tuning added to its call */
+  float trial_ms[16];         /* the trials' device times, in trial order */
+} mhsw_tuning;
+
+/* One completed mhsw_align_pairs / mhsw_align_pairs_async call, its device times in ms
+ * since the handle's initialisation (no counterpart in the reference).  The kernels of a
+ * call start once both its copies in have ended and the handle's stream has reached it
+ * (the previous call's kernels are done); copies in wait only for their input set's call
+ * two calls back. */
+typedef struct {
+  uint64_t seq;            /* call number on this handle */
+  int64_t n_pairs;
+  double copy_in_start;    /* host batches: the first copy in starts (-1 for device batches) */
+  double copy_in_end;      /* the last copy in ends (-1 for device batches) */
+  double stream_ready;     /* the handle's stream reached the call */
+  double translated;       /* translation to base codes done */
+  double forward_done;     /* forward pass done */
+  double begin_done;       /* begin pass done */
+  double done;             /* results copied out: the call is complete */
+} mhsw_call_record;
 
 typedef struct {
   int32_t max_b_len;       /* longest B (SSW query) the kernels accept */
@@ -228,13 +269,26 @@ int mhsw_align_pairs(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, i
  * another's work (klign overlaps its blocks the same way, src/klign.cpp:552-606): the
  * first enqueues the whole call -- copies in, kernels, the copy of out5 -- and returns;
  * mhsw_align_wait completes every call still pending (errors, timing, CIGAR rounds) and
- * must come before their out5 are read.  A handle keeps up to two host batches in flight
- * on two device input sets: a batch's copies wait only for the call two back, so they run
- * while the previous call's kernels do (kernels stay in call order); a third call first
+ * must come before their out5 are read.  A handle keeps up to three host batches in
+ * flight on three device input sets: a batch's copies wait only for the call three back,
+ * so they run while earlier calls' kernels do (kernels stay in call order), and a copy the
+ * host runs slowly is absorbed by the calls queued behind it; a fourth call first
  * completes the oldest.  Host arrays and out5 stay untouched by the caller until completed,
  * and should be pinned for the copies to run asynchronously.  In score2 or CIGAR mode, for
  * device batches, and on any other call on the handle, pending calls complete first. */
 int mhsw_align_pairs_async(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form);
+/* The records of the handle's last completed batch calls (at most 64 kept), oldest first:
+ * min(max_records, kept) records into out, their number into *count.  Completes pending
+ * calls first. */
+int mhsw_call_history(mhsw_driver *drv, mhsw_call_record *out, int max_records, int *count);
+/* The batched form's current configuration and last tuning (mhsw_tuning above). */
+int mhsw_last_tuning(mhsw_driver *drv, mhsw_tuning *out);
+/* Fixes the batched form's configuration and turns the tuner off: threads_per_block 64,
+ * 128 or 256; blocks_per_sm 0 (occupancy limit) or a cap; lane_rows 128 or 160;
+ * wide_try16 0 or 1 (mhsw_tuning).  threads_per_block 0 turns the tuner back on (the next
+ * batched call re-tunes).  MHSW_ERR_ARG for other values. */
+int mhsw_driver_fix_batch_config(mhsw_driver *drv, int threads_per_block, int blocks_per_sm, int lane_rows,
+                                 int wide_try16);
 int mhsw_align_wait(mhsw_driver *drv);
 int mhsw_last_timing(mhsw_driver *drv, mhsw_timing *out);
 

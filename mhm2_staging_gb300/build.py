@@ -3,6 +3,8 @@
 Outputs (git-ignored, under mhm2_staging_gb300/_build/):
   libmhsw.so      the CUDA kernels + host driver behind include/mhsw.h (sm_103a)
   libmhsw_gen.so  seeded synthetic workload generators (host C++)
+  klign_block_bench  klign's GPU call sequence through the C++ drop-in header
+                  (include/adept-sw/driver.hpp) on 20,000-pair blocks, timed (bench.py)
 
 Translation units are compiled in parallel; a unit is rebuilt only when its source or
 any header in csrc/ or include/ is newer than its object.
@@ -86,7 +88,13 @@ def build(verbose: bool = False, jobs: int | None = None) -> dict[str, Path]:
     lib = BUILD / "libmhsw.so"
     if _stale(lib, objs, 0.0):
         _run([nvcc, *ARCH_FLAGS, "-shared", "-o", str(lib), *map(str, objs), "-cudart", "static"])
-    return {"libmhsw": lib, "libmhsw_gen": gen}
+    bench = BUILD / "klign_block_bench"
+    bsrc = CSRC / "klign_block_bench.cpp"
+    if _stale(bench, [bsrc, lib], hdr):
+        cxx = os.environ.get("CXX", "g++")
+        _run([cxx, "-O2", "-std=c++14", "-I", str(INCLUDE), str(bsrc), "-o", str(bench), str(lib),
+              f"-Wl,-rpath,{BUILD}"])
+    return {"libmhsw": lib, "libmhsw_gen": gen, "klign_block_bench": bench}
 
 
 def lib_path() -> Path:
@@ -95,6 +103,10 @@ def lib_path() -> Path:
 
 def gen_lib_path() -> Path:
     return BUILD / "libmhsw_gen.so"
+
+
+def block_bench_path() -> Path:
+    return BUILD / "klign_block_bench"
 
 
 if __name__ == "__main__":

@@ -11,6 +11,7 @@
 // score could exceed the int16 range (min(lenA, lenB) * match above the int16
 // capacity) are sent straight to the int32 list.
 #include <algorithm>
+#include <chrono>
 #include <cub/cub.cuh>
 
 #include "mhsw_batch.h"
@@ -23,27 +24,45 @@ namespace mhsw {
 namespace {
 
 constexpr int kKeyShift = 17;
+constexpr int kSortBits = 20;  // 3 bucket bits above the 17 B-length bits
 // Buckets: 0..3 = A up to 64/96/128/160 rows (8-lane groups, K = 4/6/8/10),
 // 4/5 = up to 192/256 rows (16-lane groups, K = 6/8), 6 = longer A (K = 8 strips),
-// 7 = could exceed the int16 keys: straight to the int32 list.
+// 7 = could exceed the int16 keys: straight to the int32 list.  The tuned row threshold
+// (lane_rows, 160 or 128) moves A of 129..160 rows between bucket 3 and bucket 4.
 constexpr int kBucketFirstLong = 4;
 constexpr int kBucketStrip = 6;
 constexpr int kBucketWide = 7;
+constexpr int kBuckets = 8;
+constexpr int64_t kTuneSample = 256 * 1024;  // pairs the tuner's trials run on, at most
 
-__device__ __forceinline__ int bucket_of(int M, int N, const Scoring &sc) {
-  const int K = keyed_k_for_rows(M);
-  const long long bound = (long long)(M < N ? M : N) * sc.match;
-  if (bound > keyed_cap(K)) return kBucketWide;
-  return M <= 64 ? 0 : M <= 96 ? 1 : M <= 128 ? 2 : M <= 160 ? 3 : M <= 192 ? 4 : M <= 256 ? 5 : kBucketStrip;
+__host__ __device__ constexpr int bucket_k(int b) {
+  return b == 0 ? 4 : b == 1 ? 6 : b == 2 ? 8 : b == 3 ? 10 : b == 4 ? 6 : 8;
 }
 
-__global__ void k_keys(PairSet ps, Scoring sc, uint32_t *keys, uint32_t *idx) {
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < ps.n; p += (int64_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ int bucket_of(int M, int N, const Scoring &sc, int lane_rows, bool wide_try16) {
+  const int b = M <= lane_rows ? (M <= 64 ? 0 : M <= 96 ? 1 : M <= 128 ? 2 : 3)
+                               : (M <= 192 ? 4 : M <= 256 ? 5 : kBucketStrip);
+  // wide_try16: the int16 engine's ceiling test sends the pairs that do overflow to int32.
+  // That test sees a score cross the keys' capacity only if the first cell above it still
+  // fits a 16-bit key: the capacity leaves 64 values of margin and H grows by at most match
+  // per step, so it holds for match <= 63; larger matches keep the bound routing.
+  const long long bound = (long long)(M < N ? M : N) * sc.match;
+  if ((!wide_try16 || sc.match > 63) && bound > keyed_cap(bucket_k(b))) return kBucketWide;
+  return b;
+}
+
+// Sort keys of items i < m, item i = pair i * stride (stride 1: the whole batch; larger:
+// the tuner's sample); hist (the sample) counts the items per bucket.
+__global__ void k_keys(PairSet ps, Scoring sc, int lane_rows, bool wide_try16, int64_t m, int64_t stride,
+                       uint32_t *keys, uint32_t *idx, int *hist) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = i * stride;
     const int M = ps.a_len[p], N = ps.b_len[p];
-    const int b = (M <= 0 || N <= 0) ? 0 : bucket_of(M, N, sc);
+    const int b = (M <= 0 || N <= 0) ? 0 : bucket_of(M, N, sc, lane_rows, wide_try16);
     const int nb = N < 0 ? 0 : (N > 131071 ? 131071 : N);
-    keys[p] = ((uint32_t)b << kKeyShift) | (uint32_t)(131071 - nb);
-    idx[p] = (uint32_t)p;
+    keys[i] = ((uint32_t)b << kKeyShift) | (uint32_t)(131071 - nb);
+    idx[i] = (uint32_t)p;
+    if (hist) atomicAdd(&hist[b], 1);
   }
 }
 
@@ -175,30 +194,69 @@ cudaError_t grow(T **p, size_t n) {
 }  // namespace
 
 void BatchState::release() {
-  if (keys_in) cudaFree(keys_in);
-  if (keys_out) cudaFree(keys_out);
-  if (idx_in) cudaFree(idx_in);
-  if (idx_out) cudaFree(idx_out);
-  if (temp) cudaFree(temp);
+  for (uint32_t **q : {&keys_in, &keys_out, &idx_in, &idx_out, &s_keys_in, &s_keys_out, &s_idx_in, &s_idx_out}) {
+    if (*q) cudaFree(*q);
+    *q = nullptr;
+  }
+  for (void **q : {&temp, &s_temp, &scratch}) {
+    if (*q) cudaFree(*q);
+    *q = nullptr;
+  }
   if (queue) cudaFree(queue);
-  if (scratch) cudaFree(scratch);
-  keys_in = keys_out = idx_in = idx_out = nullptr;
-  temp = nullptr;
+  if (s_hist) cudaFree(s_hist);
   queue = nullptr;
-  scratch = nullptr;
+  s_hist = nullptr;
   cap = 0;
   temp_bytes = 0;
+  s_temp_bytes = 0;
   scratch_bytes = 0;
 }
 
+int signature_class(int a_len) {
+  return a_len <= 64 ? 0 : a_len <= 96 ? 1 : a_len <= 128 ? 2 : a_len <= 160 ? 3 : a_len <= 192 ? 4 : a_len <= 256 ? 5
+         : a_len <= 1024 ? 6 : 7;
+}
+
+BatchSignature batch_signature(const int32_t *a_len, int64_t n, int max_a, int max_b) {
+  BatchSignature s;
+  s.max_a_class = signature_class(max_a);
+  s.max_a = max_a;
+  s.max_b = max_b;
+  s.n = n;
+  if (a_len && n > 0) {
+    const int64_t step = n > 4096 ? n / 4096 : 1;
+    int cnt[kSigClasses] = {0};
+    int64_t k = 0;
+    for (int64_t i = 0; i < n; i += step, k++) cnt[signature_class(a_len[i])]++;
+    for (int c = 0; c < kSigClasses; c++) s.a_mix[c] = (float)cnt[c] / (float)k;
+  }
+  return s;
+}
+
+static bool within(double x, double y, double factor) {
+  x = x > 1 ? x : 1;
+  y = y > 1 ? y : 1;
+  return x <= y * factor && y <= x * factor;
+}
+
+bool BatchSignature::close_to(const BatchSignature &o) const {
+  if (max_a_class != o.max_a_class || !within(max_b, o.max_b, 2.0)) return false;
+  if (!(n < 65536 && o.n < 65536) && !within((double)n, (double)o.n, 8.0)) return false;
+  if (a_mix[0] < 0 || o.a_mix[0] < 0) return true;  // a mix the host cannot see is not compared
+  for (int c = 0; c < kSigClasses; c++)
+    if (a_mix[c] - o.a_mix[c] > kTolerance || o.a_mix[c] - a_mix[c] > kTolerance) return false;
+  return true;
+}
+
 int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultSet &rs, const WorkLists &wl,
-                    const Scoring &sc, int ceiling, int max_a, int max_b, cudaStream_t st, int64_t *launches,
-                    const Forks *fk) {
+                    const Scoring &sc, int ceiling, int max_a, int max_b, const BatchSignature &sig,
+                    cudaStream_t st, int64_t *launches, const Forks *fk) {
   auto fail = [&](cudaError_t e, const char *what) {
     bs.err = std::string(what) + ": " + cudaGetErrorString(e);
     return 1;
   };
   const int64_t n = ps.n;
+  bs.tune.last_call_tuned = false;
   if (n <= 0) return 0;
   if (n > 0x7fffffff) {
     bs.err = "batch larger than 2^31 pairs";
@@ -211,15 +269,17 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
         (e = grow(&bs.idx_out, c)))
       return fail(e, "cudaMalloc batch keys");
     size_t tb = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, tb, bs.keys_in, bs.keys_out, bs.idx_in, bs.idx_out, (int)c, 0, 20, st);
+    cub::DeviceRadixSort::SortPairs(nullptr, tb, bs.keys_in, bs.keys_out, bs.idx_in, bs.idx_out, (int)c, 0, kSortBits,
+                                    st);
     if (bs.temp) cudaFree(bs.temp);
     bs.temp = nullptr;
     if ((e = cudaMalloc(&bs.temp, tb))) return fail(e, "cudaMalloc sort temp");
     bs.temp_bytes = tb;
     bs.cap = c;
   }
-  if (!bs.queue && (e = cudaMalloc(&bs.queue, sizeof(int) * 4))) return fail(e, "cudaMalloc queue");
-  // queue[0], queue[1]: claim counters of the short and long ranges; queue[2]: split item
+  // queue[0], queue[1]: claim counters of the short and long ranges; queue[2]: split item;
+  // queue[4..6]: the same for the tuner's sample
+  if (!bs.queue && (e = cudaMalloc(&bs.queue, sizeof(int) * 8))) return fail(e, "cudaMalloc queue");
 
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -236,21 +296,25 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
   // strip scratch stride: B, the lane skew and score2 mode's zero-score padding (< 16)
   const int bcap = ((pad + std::max(max_b, 1) + 16 + 2 * kGKLong) + 15) / 16 * 16;
 
-  // keys + sort (the order is reused by every tuning trial)
-  {
-    int grid = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sms * 32);
-    k_keys<<<grid, 256, 0, st>>>(ps, sc, bs.keys_in, bs.idx_in);
+  // keys + device sort of m items (pair i * stride), split point into q[2]
+  auto sort_items = [&](const BatchShape &sh, int64_t m, int64_t stride, uint32_t *kin, uint32_t *kout, uint32_t *iin,
+                        uint32_t *iout, void *temp, size_t temp_bytes, int *q, int *hist) -> int {
+    const int grid = (int)std::min<int64_t>((m + 255) / 256, (int64_t)sms * 32);
+    if (hist && (e = cudaMemsetAsync(hist, 0, sizeof(int) * kBuckets, st))) return fail(e, "memset");
+    k_keys<<<grid, 256, 0, st>>>(ps, sc, sh.lane_rows, sh.wide_try16, m, stride, kin, iin, hist);
     if ((e = cudaGetLastError())) return fail(e, "keys launch");
-    size_t tb = bs.temp_bytes;
-    e = cub::DeviceRadixSort::SortPairs(bs.temp, tb, bs.keys_in, bs.keys_out, bs.idx_in, bs.idx_out, (int)n, 0, 20,
-                                        st);
+    size_t tb = temp_bytes;
+    e = cub::DeviceRadixSort::SortPairs(temp, tb, kin, kout, iin, iout, (int)m, 0, kSortBits, st);
     if (e) return fail(e, "radix sort");
-    k_split<<<1, 1, 0, st>>>(bs.keys_out, n, bs.queue + 2);
+    k_split<<<1, 1, 0, st>>>(kout, m, q + 2);
     if ((e = cudaGetLastError())) return fail(e, "split launch");
     if (launches) *launches += 2 + 4;  // keys, split, and the radix sort's passes (approximate)
-  }
+    return 0;
+  };
 
-  auto run = [&](const BatchShape &sh, float *ms) -> int {
+  // the two persistent launches over m sorted items (keys, order), claim counters in q
+  auto run = [&](const BatchShape &sh, const uint32_t *keys, const uint32_t *order, int64_t m, int *q,
+                 float *ms) -> int {
     const int threads = sh.groups_per_block * 8;  // block size: 8 groups of 8 lanes or 4 of 16, etc.
     const int gpb_s = threads / kGKShort, gpb_l = threads / kGKLong;
     const size_t smem_s = (size_t)gpb_s * prof_short, smem_l = (size_t)gpb_l * prof_long;
@@ -284,14 +348,14 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
       cudaEventCreate(&t1);
       cudaEventRecord(t0, st);
     }
-    cudaMemsetAsync(bs.queue, 0, 2 * sizeof(int), st);
+    cudaMemsetAsync(q, 0, 2 * sizeof(int), st);
     cudaMemsetAsync(wl.ovf_count, 0, sizeof(int), st);
     const bool fan = fk && fk->fork;
     if (fan && (e2 = fork_to(*fk, st, 1))) return fail(e2, "fork");
-    klong<<<grid_l, threads, smem_l, fan ? fk->side[0] : st>>>(ps, rs, sc, bs.keys_out, bs.idx_out, n, bs.queue,
-                                                               bs.queue + 2, ceiling, wl, pad, bcap, scr, stride);
-    kshort<<<grid_s, threads, smem_s, st>>>(ps, rs, sc, bs.keys_out, bs.idx_out, n, bs.queue, bs.queue + 2, ceiling,
-                                             wl, pad, bcap, nullptr, stride);
+    klong<<<grid_l, threads, smem_l, fan ? fk->side[0] : st>>>(ps, rs, sc, keys, order, m, q, q + 2, ceiling, wl, pad,
+                                                               bcap, scr, stride);
+    kshort<<<grid_s, threads, smem_s, st>>>(ps, rs, sc, keys, order, m, q, q + 2, ceiling, wl, pad, bcap, nullptr,
+                                             stride);
     e2 = cudaGetLastError();
     if (e2) return fail(e2, "persistent forward launch");
     if (fan && (e2 = join_from(*fk, st, 1))) return fail(e2, "join");
@@ -306,26 +370,94 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     return 0;
   };
 
-  if (bs.autotune && !bs.tuned) {
-    // Candidate launch shapes: groups per block x blocks per SM.
-    // shapes: block size (groups_per_block * 8 threads) x blocks per SM (0 = occupancy limit)
-    const BatchShape cands[] = {{8, 0}, {16, 0}, {32, 0}, {16, 2}, {32, 1}};
-    float best = 1e30f;
-    BatchShape pick = bs.shape;
-    bs.tune_n = 0;
-    for (const auto &c : cands) {
+  if (bs.autotune && (!bs.tuned || !sig.close_to(bs.tuned_for))) {
+    // Trials on a strided sample of the batch (every stride-th pair, so its length mix is
+    // the batch's), sorted as the batch is.  Coordinate descent: the launch shape at the
+    // default row threshold; then the 16-lane threshold for A of 129..160 rows; then the
+    // int16/int32 split of pairs whose bound exceeds the int16 keys -- each only when the
+    // sample has pairs it affects.  Trial results land in the result arrays of the sampled
+    // pairs and are overwritten by the batch's own pass.
+    const auto t_start = std::chrono::steady_clock::now();
+    const int64_t stride = (n + kTuneSample - 1) / kTuneSample;
+    const int64_t m = (n + stride - 1) / stride;
+    if (!bs.s_keys_in) {
+      const size_t c = (size_t)kTuneSample + 1024;
+      if ((e = grow(&bs.s_keys_in, c)) || (e = grow(&bs.s_keys_out, c)) || (e = grow(&bs.s_idx_in, c)) ||
+          (e = grow(&bs.s_idx_out, c)) || (e = grow(&bs.s_hist, (size_t)kBuckets)))
+        return fail(e, "cudaMalloc tuner sample");
+      size_t tb = 0;
+      cub::DeviceRadixSort::SortPairs(nullptr, tb, bs.s_keys_in, bs.s_keys_out, bs.s_idx_in, bs.s_idx_out, (int)c, 0,
+                                      kSortBits, st);
+      if ((e = cudaMalloc(&bs.s_temp, tb))) return fail(e, "cudaMalloc tuner sort temp");
+      bs.s_temp_bytes = tb;
+    }
+    int *sq = bs.queue + 4;
+    int hist[kBuckets] = {0};
+    auto sample_sort = [&](const BatchShape &sh) -> int {
+      if (sort_items(sh, m, stride, bs.s_keys_in, bs.s_keys_out, bs.s_idx_in, bs.s_idx_out, bs.s_temp,
+                     bs.s_temp_bytes, sq, bs.s_hist))
+        return 1;
+      if ((e = cudaMemcpyAsync(hist, bs.s_hist, sizeof(hist), cudaMemcpyDeviceToHost, st)) ||
+          (e = cudaStreamSynchronize(st)))
+        return fail(e, "tuner histogram");
+      return 0;
+    };
+    TuneRecord tr;
+    tr.tunings = bs.tune.tunings + 1;
+    tr.sample_pairs = m;
+    auto trial = [&](const BatchShape &sh, float *ms) -> int {
+      if (run(sh, bs.s_keys_out, bs.s_idx_out, m, sq, ms)) return 1;
+      if (tr.trials < 16) tr.trial_ms[tr.trials] = *ms;
+      tr.trials++;
+      return 0;
+    };
+    BatchShape best;  // defaults: 128-thread blocks, occupancy limit, rows <= 160 in 8-lane groups
+    if (sample_sort(best)) return 1;
+    float warm = 0.f, best_ms = 1e30f;
+    if (run(best, bs.s_keys_out, bs.s_idx_out, m, sq, &warm)) return 1;  // untimed warm-up
+    const BatchShape shapes[] = {{8, 0}, {16, 0}, {32, 0}, {16, 2}, {32, 1}};
+    for (const BatchShape &c0 : shapes) {
+      BatchShape c = best;
+      c.groups_per_block = c0.groups_per_block;
+      c.blocks_per_sm = c0.blocks_per_sm;
       float ms = 0.f;
-      if (run(c, &ms)) return 1;
-      if (bs.tune_n < 8) bs.tune_ms[bs.tune_n++] = ms;
-      if (ms < best) {
-        best = ms;
-        pick = c;
+      if (trial(c, &ms)) return 1;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
       }
     }
-    bs.shape = pick;
+    if (hist[3] > 0) {  // A of 129..160 rows present: try them in 16-lane groups
+      BatchShape c = best;
+      c.lane_rows = 128;
+      float ms = 0.f;
+      if (sample_sort(c) || trial(c, &ms)) return 1;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+      if (sample_sort(best)) return 1;  // hist of the kept threshold
+    }
+    if (hist[kBucketWide] > 0 && sc.match <= 63) {  // bound above the int16 keys: try int16 first
+      BatchShape c = best;
+      c.wide_try16 = true;
+      float ms = 0.f;
+      if (sample_sort(c) || trial(c, &ms)) return 1;
+      if (ms < best_ms) best = c;
+    }
+    bs.shape = best;
+    bs.tuned_for = sig;
     bs.tuned = true;
+    tr.last_call_tuned = true;
+    tr.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    bs.tune = tr;
   }
-  return run(bs.shape, nullptr);
+
+  // the batch: keys with the kept configuration, sort, the persistent launches
+  if (sort_items(bs.shape, n, 1, bs.keys_in, bs.keys_out, bs.idx_in, bs.idx_out, bs.temp, bs.temp_bytes, bs.queue,
+                 nullptr))
+    return 1;
+  return run(bs.shape, bs.keys_out, bs.idx_out, n, bs.queue, nullptr);
 }
 
 }  // namespace mhsw

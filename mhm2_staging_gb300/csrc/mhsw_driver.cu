@@ -8,12 +8,16 @@
 //   * buffers grow with the batch (no fixed KLIGN_GPU_BLOCK_SIZE cap, driver.cpp:213-242);
 //   * sequences travel as raw bytes and are translated on the device with SSW's table.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mhsw.h"
@@ -79,6 +83,89 @@ constexpr int kInt16Ceiling = mhsw::V16::kBig - 1 - 64;  // leaves room for one 
 
 }  // namespace
 
+// A few host threads a handle keeps for copying a batch's strings into its pinned staging
+// buffers: klign hands each block over as std::vector<std::string> (about 13 MB for
+// 20,000 reads and windows), and one thread copying them took longer than the block's
+// kernels.  run(parts, fn) calls fn(0 .. parts-1) on the pool's threads and the caller's
+// and returns when every part is done and no pool thread is still inside the job.
+class CopyPool {
+ public:
+  ~CopyPool() {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      quit_ = true;
+    }
+    cv_.notify_all();
+    for (std::thread &t : th_) t.join();
+  }
+  static int threads_wanted() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    return hw > 2 ? (int)std::min(8u, hw - 1) : 0;
+  }
+  void run(int parts, const std::function<void(int)> &fn) {
+    if (th_.empty()) {
+      const int k = threads_wanted();
+      for (int i = 0; i < k; i++) th_.emplace_back([this] { loop(); });
+    }
+    if (th_.empty() || parts <= 1) {
+      for (int p = 0; p < parts; p++) fn(p);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      job_ = &fn;
+      total_ = parts;
+      next_.store(0);
+      finished_.store(0);
+      gen_++;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(m_);
+    done_cv_.wait(lk, [this] { return finished_.load() == total_ && busy_ == 0; });
+    job_ = nullptr;
+  }
+
+ private:
+  void work() {
+    for (;;) {
+      const int p = next_.fetch_add(1);
+      if (p >= total_) return;
+      (*job_)(p);
+      if (finished_.fetch_add(1) + 1 == total_) {
+        std::lock_guard<std::mutex> lk(m_);
+        done_cv_.notify_all();
+      }
+    }
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_.wait(lk, [&] { return quit_ || gen_ != seen; });
+        if (quit_) return;
+        seen = gen_;
+        busy_++;
+      }
+      work();
+      {
+        std::lock_guard<std::mutex> lk(m_);
+        busy_--;
+      }
+      done_cv_.notify_all();
+    }
+  }
+  std::mutex m_;
+  std::condition_variable cv_, done_cv_;
+  std::vector<std::thread> th_;
+  const std::function<void(int)> *job_ = nullptr;
+  int total_ = 0, busy_ = 0;
+  std::atomic<int> next_{0}, finished_{0};
+  uint64_t gen_ = 0;
+  bool quit_ = false;
+};
+
 struct mhsw_driver {
   std::mutex mu;
   std::mutex call_mu;  // calls on the call arena (caller side, protein), whole-call
@@ -108,6 +195,8 @@ struct mhsw_driver {
   DBuf<unsigned char> outv;  // 5 x int16 + 5 x int32 arrays
   DBuf<int32_t> out5;
   mhsw::BatchState batch;     // batched-form work buffers
+  CopyPool copy_pool;         // host threads for staging a block's strings
+  mhsw::BatchSignature sig;   // length signature of the batch being aligned (the tuner's key)
   // score2 mode: SSW's second-best score per pair (row maxima arenas, results)
   bool score2 = false;
   int64_t score2_n = -1;  // pairs of the last batch whose second-best scores are in r_score2
@@ -133,29 +222,40 @@ struct mhsw_driver {
   DBuf<unsigned char> c_pool, c_temp;
   HBuf<int> h_ccounts;
   cudaEvent_t ev_c[2] = {nullptr, nullptr};
-  // Batch calls enqueued (mhsw_align_pairs_async) and not yet completed: up to two, in
-  // two slots used in turn.  A host batch copies into its slot's input set on the copy
-  // streams, which wait only for that set's previous call (two calls back), so its copies
-  // run while the previous call's kernels do; kernels stay in order on the handle's stream.
+  // Batch calls enqueued (mhsw_align_pairs_async) and not yet completed: up to kSlots,
+  // in slots used in turn.  A host batch copies into its slot's input set on the copy
+  // streams, which wait only for that set's previous call (kSlots calls back), so its
+  // copies run while earlier calls' kernels do, and a copy that runs slow (the host's copy
+  // rate drops on some calls) is absorbed by the calls queued behind it; kernels stay in
+  // order on the handle's stream.
+  static constexpr int kSlots = 3;
   struct Pending {
     bool active = false;
     int64_t n = 0;
     double cells = 0;
     uint64_t seq = 0;
     mhsw::PairSet ps;
-  } pend[2];
+  } pend[kSlots];
   struct InSet {
     DBuf<char> a_seq, b_seq;
     DBuf<int64_t> a_off, b_off;
     DBuf<int32_t> a_len, b_len;
     cudaEvent_t free_ev = nullptr;  // recorded after the kernels of the set's last call
     bool used = false;
-  } in_sets[2];
+  } in_sets[kSlots];
   static constexpr int kCopyStreams = 4;
   cudaStream_t copy_st[kCopyStreams] = {};
   cudaEvent_t copy_ev[kCopyStreams] = {};
-  cudaEvent_t ev_p[2][5] = {};  // per slot: phase events of its call
-  HBuf<int> h_counts_p[2];       // per slot: the call's counters
+  cudaEvent_t ev_p[kSlots][5] = {};  // per slot: phase events of its call
+  // per slot: its copies in start (copy stream 0) and end (one per copy stream); the
+  // handle's epoch (recorded at init) that the call records are timed from
+  cudaEvent_t ev_cin[kSlots][1 + kCopyStreams] = {};
+  bool cin_recorded[kSlots] = {};
+  cudaEvent_t ev_epoch = nullptr;
+  static constexpr int kHistory = 64;
+  mhsw_call_record history[kHistory] = {};
+  int64_t history_n = 0;  // records written so far (the ring keeps the last kHistory)
+  HBuf<int> h_counts_p[kSlots];  // per slot: the call's counters
   int next_slot = 0;
   uint64_t call_seq = 0;
 
@@ -277,6 +377,10 @@ struct mhsw_driver {
     for (auto &row : ev_p)
       for (auto &e : row)
         if (e) cudaEventDestroy(e);
+    for (auto &row : ev_cin)
+      for (auto &e : row)
+        if (e) cudaEventDestroy(e);
+    if (ev_epoch) cudaEventDestroy(ev_epoch);
     for (auto &h : h_counts_p) h.release();
     h_a.release();
     h_b.release();
@@ -587,8 +691,8 @@ int forward_passes(mhsw_driver *d, const mhsw::PairSet &ps, int max_a, int max_b
   mhsw::WorkLists wl = work_lists(d, ps.n);
   MHSW_CK(mhsw::reset_lists(wl, d->st), "reset lists");
   d->launches += 1;
-  if (mhsw::batched_forward(d->batch, d->device, ps, result_set(d), wl, d->sc, ceiling_for(d), max_a, max_b, d->st,
-                            &d->launches, &d->forks))
+  if (mhsw::batched_forward(d->batch, d->device, ps, result_set(d), wl, d->sc, ceiling_for(d), max_a, max_b, d->sig,
+                            d->st, &d->launches, &d->forks))
     return d->fail(MHSW_ERR_CUDA, "batched forward: %s", d->batch.err.c_str());
   d->fwd_order = d->batch.idx_out;
   // int32 pass over the pairs the int16 engine could not hold
@@ -680,11 +784,19 @@ int stage_strings(mhsw_driver *d, const char *const *reads, const int32_t *read_
     d->h_boff.p[i] = ob;
     d->h_alen.p[i] = al[i];
     d->h_blen.p[i] = bl[i];
-    if (al[i]) memcpy(d->h_a.p + oa, as[i], (size_t)al[i]);
-    if (bl[i]) memcpy(d->h_b.p + ob, bs[i], (size_t)bl[i]);
     oa += al[i];
     ob += bl[i];
   }
+  // the bytes, in parts of about 1 MB on the handle's copy threads
+  const int parts = (int)std::min<int64_t>(std::max<int64_t>((ta + tb) >> 20, 1), std::max(n, 1));
+  const std::function<void(int)> copy_part = [&](int part) {
+    const int32_t lo = (int32_t)((int64_t)n * part / parts), hi = (int32_t)((int64_t)n * (part + 1) / parts);
+    for (int32_t i = lo; i < hi; i++) {
+      if (al[i]) memcpy(d->h_a.p + d->h_aoff.p[i], as[i], (size_t)al[i]);
+      if (bl[i]) memcpy(d->h_b.p + d->h_boff.p[i], bs[i], (size_t)bl[i]);
+    }
+  };
+  d->copy_pool.run(parts, copy_part);
   int rc = ensure_device(d, n, ta, tb);
   if (rc) return rc;
   rc = ensure_results(d, n);
@@ -726,7 +838,7 @@ mhsw::PairSet staged_pairs(mhsw_driver *d) {
 // work on the handle's stream, so the copies overlap the previous call's kernels;
 // otherwise they wait for everything issued on the handle's stream so far.
 int copy_batch_in(mhsw_driver *d, mhsw_driver::InSet &in, const mhsw_pairs *pairs, int64_t n, int64_t ta,
-                  int64_t tb, bool after_free) {
+                  int64_t tb, bool after_free, int slot) {
   constexpr size_t kPiece = size_t(64) << 20;
   constexpr int kLanes = mhsw_driver::kCopyStreams;
   if (!after_free) MHSW_CK(cudaEventRecord(d->copy_ev[0], d->st), "event");
@@ -737,6 +849,7 @@ int copy_batch_in(mhsw_driver *d, mhsw_driver::InSet &in, const mhsw_pairs *pair
       MHSW_CK(cudaStreamWaitEvent(d->copy_st[k], d->copy_ev[0], 0), "wait stream");
     }
   }
+  MHSW_CK(cudaEventRecord(d->ev_cin[slot][0], d->copy_st[0]), "event");
   int lane = 0;
   auto put = [&](void *dst, const void *src, size_t len) -> cudaError_t {
     for (size_t o = 0; o < len; o += kPiece) {
@@ -755,9 +868,11 @@ int copy_batch_in(mhsw_driver *d, mhsw_driver::InSet &in, const mhsw_pairs *pair
   MHSW_CK(put(in.a_len.p, pairs->a_len, sizeof(int32_t) * n), "H2D");
   MHSW_CK(put(in.b_len.p, pairs->b_len, sizeof(int32_t) * n), "H2D");
   for (int k = 0; k < kLanes; k++) {
+    MHSW_CK(cudaEventRecord(d->ev_cin[slot][1 + k], d->copy_st[k]), "event");
     MHSW_CK(cudaEventRecord(d->copy_ev[k], d->copy_st[k]), "event");
     MHSW_CK(cudaStreamWaitEvent(d->st, d->copy_ev[k], 0), "wait copies");
   }
+  d->cin_recorded[slot] = true;
   return MHSW_OK;
 }
 
@@ -876,6 +991,10 @@ int mhsw_driver_init(mhsw_driver *d, int rank_me, int rank_n, short match_score,
   for (auto &e : d->ev_c) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
   for (auto &row : d->ev_p)
     for (auto &e : row) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
+  for (auto &row : d->ev_cin)
+    for (auto &e : row) MHSW_CK(cudaEventCreate(&e), "cudaEventCreate");
+  MHSW_CK(cudaEventCreate(&d->ev_epoch), "cudaEventCreate");
+  MHSW_CK(cudaEventRecord(d->ev_epoch, d->st), "event");
   for (auto &in : d->in_sets) MHSW_CK(cudaEventCreateWithFlags(&in.free_ev, cudaEventDisableTiming), "cudaEventCreate");
   for (auto &c : d->copy_st) MHSW_CK(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking), "cudaStreamCreate");
   for (auto &e : d->copy_ev) MHSW_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
@@ -964,6 +1083,8 @@ int mhsw_run_kernel_forwards(mhsw_driver *d, const char *const *reads, const int
   MHSW_CK(cudaEventRecord(d->ev_t[0], d->st), "event");
   rc = stage_strings(d, reads, read_lens, contigs, contig_lens, n);
   if (rc) return rc;
+  d->sig = mhsw::batch_signature(d->orientation == MHSW_ORIENT_KLIGN ? read_lens : contig_lens, n, d->max_a,
+                                 d->max_b);
   mhsw::PairSet ps = staged_pairs(d);
   if (n > 0) {
     rc = translate_batch(d, &ps, d->a_bytes, d->b_bytes);
@@ -1169,16 +1290,36 @@ int finish_slot(mhsw_driver *d, int s) {
   d->timing.graph_replays = d->graph_launches;
   d->timing.cigar_ms = d->cigar_ms;
   d->timing.n_cigar_generic = d->cigar_generic;
+  // the call's record, ms since the handle's epoch
+  mhsw_call_record r{};
+  r.seq = pd.seq;
+  r.n_pairs = n;
+  r.copy_in_start = r.copy_in_end = -1;
+  if (d->cin_recorded[s]) {
+    r.copy_in_start = elapsed(d->ev_epoch, d->ev_cin[s][0]);
+    for (int k = 0; k < mhsw_driver::kCopyStreams; k++)
+      r.copy_in_end = std::max(r.copy_in_end, (double)elapsed(d->ev_epoch, d->ev_cin[s][1 + k]));
+  }
+  r.stream_ready = elapsed(d->ev_epoch, ev[0]);
+  r.translated = elapsed(d->ev_epoch, ev[1]);
+  r.forward_done = elapsed(d->ev_epoch, ev[2]);
+  r.begin_done = elapsed(d->ev_epoch, ev[3]);
+  r.done = elapsed(d->ev_epoch, ev[4]);
+  d->history[d->history_n % mhsw_driver::kHistory] = r;
+  d->history_n++;
   return MHSW_OK;
 }
 
 // Completes every pending batch call, oldest first.
 int finish_pending(mhsw_driver *d) {
-  const bool both = d->pend[0].active && d->pend[1].active;
-  const int first = both ? (d->pend[0].seq < d->pend[1].seq ? 0 : 1) : (d->pend[0].active ? 0 : 1);
-  int rc = finish_slot(d, first);
-  if (rc) return rc;
-  return finish_slot(d, 1 - first);
+  for (;;) {
+    int oldest = -1;
+    for (int k = 0; k < mhsw_driver::kSlots; k++)
+      if (d->pend[k].active && (oldest < 0 || d->pend[k].seq < d->pend[oldest].seq)) oldest = k;
+    if (oldest < 0) return MHSW_OK;
+    const int rc = finish_slot(d, oldest);
+    if (rc) return rc;
+  }
 }
 
 // Everything of a batch call up to its completion event, enqueued on the handle's stream;
@@ -1191,8 +1332,9 @@ int align_pairs_begin(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, in
   int slot = 0;
   int rc = MHSW_OK;
   if (overlap) {
+    // slots go round in call order, so the slot taken holds the oldest call in flight
     slot = d->next_slot;
-    d->next_slot ^= 1;
+    d->next_slot = (d->next_slot + 1) % mhsw_driver::kSlots;
     rc = finish_slot(d, slot);
   } else {
     rc = finish_pending(d);
@@ -1200,6 +1342,7 @@ int align_pairs_begin(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, in
   }
   if (rc) return rc;
   cudaEvent_t *ev = d->ev_p[slot];
+  d->cin_recorded[slot] = false;
   if (!pairs || pairs->n < 0 || (pairs->n > 0 && !out5)) return d->fail(MHSW_ERR_ARG, "bad pairs");
   if (form != MHSW_FORM_PLAIN && form != MHSW_FORM_BATCHED) return d->fail(MHSW_ERR_ARG, "unknown form %d", form);
   if (d->ev_live) MHSW_CK(cudaEventSynchronize(d->ev_done), "wait previous batch");
@@ -1241,7 +1384,7 @@ int align_pairs_begin(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, in
     MHSW_CK(in.a_len.reserve((size_t)n + 1), "cudaMalloc lengths");
     MHSW_CK(in.b_len.reserve((size_t)n + 1), "cudaMalloc lengths");
     if (n > 0) {
-      rc = copy_batch_in(d, in, pairs, n, ta, tb, overlap);
+      rc = copy_batch_in(d, in, pairs, n, ta, tb, overlap, slot);
       if (rc) return rc;
     }
     ps.a_seq = in.a_seq.p;
@@ -1287,7 +1430,10 @@ int align_pairs_begin(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, in
     ps.b_seq = pairs->b_seq;
     ps.b_off = pairs->b_off;
     ps.b_len = pairs->b_len;
+    d->sig = mhsw::batch_signature(la.data(), n, ma, mb);
   }
+  if (host_io) d->sig = mhsw::batch_signature(pairs->a_len, n, ma, mb);
+  else if (hinted_sizes) d->sig = mhsw::batch_signature(nullptr, n, ma, mb);
   ps.n = n;
   if (mb > mhsw::kMaxB) return d->fail(MHSW_ERR_LIMIT, "sequence of %d bytes exceeds the limit %d", mb, mhsw::kMaxB);
   rc = ensure_results(d, n);
@@ -1382,7 +1528,10 @@ int align_pairs_begin(mhsw_driver *d, const mhsw_pairs *pairs, int32_t *out5, in
     cudaGraph_t graph = nullptr;
     MHSW_CK(cudaStreamBeginCapture(d->st, cudaStreamCaptureModeThreadLocal), "begin capture");
     capturing = true;
+    const bool tune_was = d->batch.autotune;
+    d->batch.autotune = false;  // the tuner synchronises: never inside a capture
     const int r = enqueue();
+    d->batch.autotune = tune_was;
     capturing = false;
     const cudaError_t ce = cudaStreamEndCapture(d->st, &graph);
     if (r || ce != cudaSuccess || !graph) {
@@ -1466,6 +1615,59 @@ int mhsw_last_timing(mhsw_driver *d, mhsw_timing *out) {
   std::lock_guard<std::mutex> lk(d->mu);
   if (int rcp = finish_pending(d)) return rcp;
   *out = d->timing;
+  return MHSW_OK;
+}
+
+int mhsw_call_history(mhsw_driver *d, mhsw_call_record *out, int max_records, int *count) {
+  if (!d || !count || max_records < 0 || (max_records > 0 && !out)) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
+  const int64_t have = std::min<int64_t>(d->history_n, mhsw_driver::kHistory);
+  const int64_t k = std::min<int64_t>(have, max_records);
+  for (int64_t i = 0; i < k; i++) out[i] = d->history[(d->history_n - k + i) % mhsw_driver::kHistory];
+  *count = (int)k;
+  return MHSW_OK;
+}
+
+int mhsw_last_tuning(mhsw_driver *d, mhsw_tuning *out) {
+  if (!d || !out) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
+  const mhsw::BatchState &b = d->batch;
+  mhsw_tuning t{};
+  t.threads_per_block = b.shape.groups_per_block * 8;
+  t.blocks_per_sm = b.shape.blocks_per_sm;
+  t.lane_rows = b.shape.lane_rows;
+  t.wide_try16 = b.shape.wide_try16 ? 1 : 0;
+  t.last_call_tuned = b.tune.last_call_tuned ? 1 : 0;
+  t.trials = b.tune.trials;
+  t.sample_pairs = b.tune.sample_pairs;
+  t.tunings = b.tune.tunings;
+  t.tune_wall_ms = b.tune.wall_ms;
+  for (int k = 0; k < 16; k++) t.trial_ms[k] = b.tune.trial_ms[k];
+  *out = t;
+  return MHSW_OK;
+}
+
+int mhsw_driver_fix_batch_config(mhsw_driver *d, int threads_per_block, int blocks_per_sm, int lane_rows,
+                                 int wide_try16) {
+  if (!d) return MHSW_ERR_ARG;
+  std::lock_guard<std::mutex> lk(d->mu);
+  if (int rcp = finish_pending(d)) return rcp;
+  if (threads_per_block == 0) {
+    d->batch.autotune = true;
+    d->batch.tuned = false;
+    return MHSW_OK;
+  }
+  if ((threads_per_block != 64 && threads_per_block != 128 && threads_per_block != 256) || blocks_per_sm < 0 ||
+      blocks_per_sm > 32 || (lane_rows != 128 && lane_rows != 160) || (wide_try16 != 0 && wide_try16 != 1))
+    return d->fail(MHSW_ERR_ARG, "batch configuration (%d, %d, %d, %d) not supported", threads_per_block,
+                   blocks_per_sm, lane_rows, wide_try16);
+  d->batch.autotune = false;
+  d->batch.shape.groups_per_block = threads_per_block / 8;
+  d->batch.shape.blocks_per_sm = blocks_per_sm;
+  d->batch.shape.lane_rows = lane_rows;
+  d->batch.shape.wide_try16 = wide_try16 != 0;
   return MHSW_OK;
 }
 
@@ -1603,6 +1805,7 @@ int align_resident(mhsw_driver *d, const PairSet &in, int64_t a_bytes, int max_a
   rc = attach_score2(d, &ps, n, a_bytes);
   if (rc) return rc;
   MHSW_CK(cudaEventRecord(d->ev_t[1], d->st), "event");
+  d->sig = mhsw::batch_signature(nullptr, ps.n, max_a, max_b);
   rc = forward_any(d, ps, max_a, max_b, form);
   if (rc) return rc;
   MHSW_CK(cudaEventRecord(d->ev_t[2], d->st), "event");

@@ -210,13 +210,16 @@ __host__ __device__ __forceinline__ int band_gap_bound(int t, int N2, int S, con
 // Band class of pair p (0 .. kBandClasses-1), kBandClasses for the wavefront, or -1 when
 // there is nothing to search (score 0, or a pair the forward pass rejected); those get
 // their begin written here.
-__device__ __forceinline__ int band_class(const ResultSet &rs, const Scoring &sc, int64_t p) {
+// s_cap: the largest score the band kernels take (the packed int16 kernels hold scores up
+// to kBand16Score); pairs above it go to the wavefront list too.
+__device__ __forceinline__ int band_class(const ResultSet &rs, const Scoring &sc, int64_t p, int s_cap) {
   const int S = rs.score[p];
   if ((rs.flag[p] & kFlagTooLong) || S <= 0) {
     rs.a_beg[p] = -1;
     rs.b_beg[p] = 0;
     return -1;
   }
+  if (S > s_cap) return kBandClasses;
   const int M2 = rs.a_end[p] + 1, N2 = rs.b_end[p] + 1;
   const int g = band_gap_bound(band_first_cap(S, sc.match, M2), N2, S, sc);
 #pragma unroll
@@ -243,13 +246,13 @@ __device__ __forceinline__ void append_agg(int64_t *list, int *count, int64_t ca
 
 // Pass 1: count the pairs of each band class.
 __global__ void __launch_bounds__(256) k_rev_count(ResultSet rs, Scoring sc, const uint32_t *__restrict__ order,
-                                                   int64_t n, int *band_counts) {
+                                                   int64_t n, int *band_counts, int s_cap) {
   __shared__ int cnt[kBandClasses];
   if (threadIdx.x < kBandClasses) cnt[threadIdx.x] = 0;
   __syncthreads();
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = order ? (int64_t)order[idx] : idx;
-    const int c = band_class(rs, sc, p);
+    const int c = band_class(rs, sc, p, s_cap);
     if (c >= 0 && c < kBandClasses) atomicAdd(&cnt[c], 1);
   }
   __syncthreads();
@@ -259,7 +262,7 @@ __global__ void __launch_bounds__(256) k_rev_count(ResultSet rs, Scoring sc, con
 // Pass 2: place each pair in its class segment (segments in class order, each filled in
 // the batch's order); wider pairs go to the wavefront list.
 __global__ void __launch_bounds__(256) k_rev_scatter(ResultSet rs, Scoring sc, const uint32_t *__restrict__ order,
-                                                     int64_t n, WorkLists wl) {
+                                                     int64_t n, WorkLists wl, int s_cap) {
   int off[kBandClasses];
   int acc = 0;
 #pragma unroll
@@ -276,9 +279,11 @@ __global__ void __launch_bounds__(256) k_rev_scatter(ResultSet rs, Scoring sc, c
       const int M2 = rs.a_end[p] + 1, N2 = rs.b_end[p] + 1;
       const int g = band_gap_bound(band_first_cap(S, sc.match, M2), N2, S, sc);
       c = kBandClasses;
+      if (S <= s_cap) {
 #pragma unroll
-      for (int k = kBandClasses - 1; k >= 0; k--)
-        if (g <= band_half(k)) c = k;
+        for (int k = kBandClasses - 1; k >= 0; k--)
+          if (g <= band_half(k)) c = k;
+      }
     }
     // one append per class present in the warp: lanes of a class share one atomic
     const unsigned act = __activemask();
@@ -415,15 +420,42 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
   for (int c = 0; c < C; c++) off += wl.band_counts[c];
   int64_t total = wl.band_counts[C];
   if (off + total > wl.cap) total = wl.cap - off;
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = wl.bands[off + idx];
-    const int S = rs.score[p];
-    const int ie = rs.a_end[p], je = rs.b_end[p];
+  // A pair's fields are loaded one grid-stride iteration ahead of its search (their
+  // chain of dependent loads then overlaps the previous pair's rows), and the A codes of
+  // each block's first row pair one block ahead (the other rows' codes are loaded at the
+  // block's start and used after the first pair; the window's new columns are first read
+  // at the end of a row).
+  struct Meta {
+    int64_t p = -1;
+    int S = 0, ie = 0, je = 0;
+    int64_t aoff = 0, boff = 0;
+  };
+  auto load_meta = [&](int64_t idx) {
+    Meta m;
+    if (idx < total) {
+      m.p = wl.bands[off + idx];
+      m.S = rs.score[m.p];
+      m.ie = rs.a_end[m.p];
+      m.je = rs.b_end[m.p];
+      m.aoff = ps.a_off[m.p];
+      m.boff = ps.b_off[m.p];
+    }
+    return m;
+  };
+  const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  Meta cur = load_meta(idx);
+  for (; idx < total; idx += gstride) {
+    const Meta nxt = load_meta(idx + gstride);
+    const int64_t p = cur.p;
+    const int S = cur.S;
+    const int ie = cur.ie, je = cur.je;
     const int M2 = ie + 1, N2 = je + 1;
-    const uint8_t *a = ps.a_code + ps.a_off[p] + ie;  // reversed: a[-i]
-    const uint8_t *b = ps.b_code + ps.b_off[p] + je;  // reversed: b[-j]
+    const uint8_t *a = ps.a_code + cur.aoff + ie;  // reversed: a[-i]
+    const uint8_t *b = ps.b_code + cur.boff + je;  // reversed: b[-j]
+    cur = nxt;
     auto code_at = [&](int j) -> int { return ((unsigned)j < (unsigned)N2 ? (int)b[-j] : kCodePad) | 0x7770; };
+    auto row_code = [&](int r) -> int { return r < M2 ? (int)a[-r] : kCodePad; };
     // row caps are kept at multiples of U (or M2) so the window always slides by U
     auto cap_rows = [&](int t) { t = (t + U - 1) / U * U; return t < M2 ? t : M2; };
     int t = cap_rows(band_first_cap(S, mt, M2));
@@ -437,6 +469,7 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
     }
 #pragma unroll
     for (int k = 0; k < NC; k++) cb[k] = code_at(k - G);
+    int a0 = row_code(0), a1 = row_code(1);  // the block's first row pair
     int i = 0;  // first row of the current block; the window covers columns i - G + [0, NC)
     for (;;) {
       if (band_gap_bound(t, N2, S, sc) > G) {
@@ -444,14 +477,15 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
         break;
       }
       while (i < t && !found) {
+        // the next block's first row pair
+        const int n0 = row_code(i + U), n1 = row_code(i + U + 1);
         // t is a multiple of U below M2, so a row pair starting below t ends below t
         // unless t == M2 (its lower row is then the PAD row)
 #pragma unroll
         for (int u = 0; u < U; u += 2) {
           const int row = i + u;
           if (!found && row < t) {
-            const int ca = a[-row];
-            const int cc = row + 1 < M2 ? (int)a[-(row + 1)] : kCodePad;
+            const int ca = u == 0 ? a0 : row_code(row), cc = u == 0 ? a1 : row_code(row + 1);
             const int km = band_pair<W, NC, BI>(cb, u, rptab[2 * ca], rptab[2 * ca + 1], rptab[2 * cc],
                                                 rptab[2 * cc + 1], bias, ngo, nge, k128, H, E);
             if ((km >> 7) >= S) {
@@ -467,6 +501,8 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
         for (int k = 0; k < W; k++) cb[k] = cb[k + U];
 #pragma unroll
         for (int k = W; k < NC; k++) cb[k] = code_at(i - G + k);
+        a0 = n0;
+        a1 = n1;
       }
       if (found || t >= M2) break;
       t = cap_rows(2 * t);
@@ -474,6 +510,189 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
     append_agg(wl.wide, wl.wide_count, wl.cap, p, escalate);
     if (escalate) continue;
     if (!found || fi >= M2 || fj < 0 || fj >= N2) {
+      rs.flag[p] |= kFlagTooLong;  // inconsistent; reported as an error by the driver
+      rs.a_beg[p] = -1;
+      rs.b_beg[p] = 0;
+      continue;
+    }
+    rs.a_beg[p] = ie - fi;
+    rs.b_beg[p] = je - fj;
+  }
+}
+
+// Packed int16x2 form of the row-pair band, for scores up to kBand16Score under the
+// gap-open-biased table (klign's scorings).  One register holds a cell of row A (low
+// half) and the cell of row B two positions behind it (high half), so each DPX operation
+// updates both rows.  After a row pair, P[k] = (H of A's cell k, H of B's cell k - 2) and
+// Q[k] likewise for E^; the next pair reads the row above from the high halves (old) and
+// its own upper row from the low halves (new), so the "above" operands of a step are
+// gathered by one byte permute each, and the diagonal operand of a step is the "above"
+// operand of the step before.  F's chain runs along each half on its own.  Halves that are
+// no cell (B before its first cell, A past its last) are kept out: A's cells past the band
+// hold H = 0 and E^ = NEG for B, and the row maxima skip both.  No cell of the reversed box
+// exceeds S (<= 16000), every value stays inside int16, and the low-half sums of the
+// multiply-add never carry (all terms are non-negative).
+constexpr int kBand16Score = 16000;
+
+template <int W, int NC>
+__device__ __forceinline__ uint32_t band_pair16(const int (&cb)[NC], int u, uint32_t ra0, uint32_t ra1,
+                                                uint32_t rb0, uint32_t rb1, uint32_t one, uint32_t ngo2,
+                                                uint32_t nge2, uint32_t (&P)[W + 3], uint32_t (&Q)[W + 3]) {
+  constexpr uint32_t NEG2 = 0xC000C000u;  // -16384 in both halves
+  uint32_t F2 = NEG2, rm = 0u, up_prev = 0u;
+#pragma unroll
+  for (int s = 0; s < W + 2; s++) {
+    // above-operands: high halves of the old row at s + 3, low halves of the new row at s - 1
+    constexpr int kLast = W + 2;
+    const int iu = s + 3 <= kLast ? s + 3 : kLast;
+    const uint32_t up2 = __byte_perm(P[iu], s >= 1 ? P[s >= 1 ? s - 1 : 0] : 0u, 0x5432);
+    const uint32_t eup2 = __byte_perm(Q[iu], s >= 1 ? Q[s >= 1 ? s - 1 : 0] : NEG2, 0x5432);
+    const uint32_t diag2 = s == 0 ? __byte_perm(P[2], 0u, 0x5432) : up_prev;
+    // scores (s + gO as bytes): A at window column u + s, B one column to the left
+    const uint32_t sa = __byte_perm(ra0, ra1, (uint32_t)cb[u + s]);
+    const uint32_t sb = __byte_perm(rb0, rb1, (uint32_t)cb[u + s >= 1 ? u + s - 1 : 0]);
+    const uint32_t q2 = mad_u32(diag2, one, __byte_perm(sa, sb, 0x5410));
+    const uint32_t e2 = __viaddmax_s16x2(eup2, nge2, up2);
+    if (s == 2) F2 = __byte_perm(F2, NEG2, 0x7610);  // B's row starts here
+    const uint32_t h2 = __viaddmax_s16x2_relu(__vimax3_s16x2(q2, e2, F2), ngo2, 0u);
+    F2 = __viaddmax_s16x2(F2, nge2, h2);
+    uint32_t hs = h2, es = e2;
+    if (s >= W) {  // A has no cell here: H = 0, E^ = NEG for the cells of B below it
+      hs = h2 & 0xffff0000u;
+      es = __byte_perm(e2, NEG2, 0x3254);
+    }
+    P[s] = hs;
+    Q[s] = es;
+    rm = __vmaxs2(rm, s < 2 ? (h2 & 0xffffu) : hs);
+    up_prev = up2;
+  }
+  return rm;
+}
+
+// Pass 3, packed: k_rev_band's search with band_pair16 (klign's scorings, S <= 16000).
+template <int WB, int C>
+__global__ void __launch_bounds__(128) k_rev_band16(PairSet ps, ResultSet rs, Scoring sc, WorkLists wl) {
+  constexpr int G = WB / 2 - 1;
+  constexpr int W = 2 * G + 1;
+  constexpr int U = W <= 15 ? 8 : (W <= 31 ? 4 : 2);
+  constexpr int NC = W + U;
+  static_assert(G == band_half(C), "band class and width disagree");
+  static_assert(U % 2 == 0, "rows go in pairs within a block");
+  __shared__ uint32_t rptab[2 * 8];
+  if (threadIdx.x < 6) {
+    const int a = threadIdx.x;
+    uint32_t r0 = 0, r1 = 0;
+    for (int c = 0; c < 5 && a < kCodePad; c++) {
+      const uint32_t v = (uint32_t)(sub_score(a, c, sc, 128) + sc.gap_open) & 0xffu;
+      if (c < 4) r0 |= v << (8 * c);
+      else r1 = v;
+    }
+    rptab[2 * a] = r0;
+    rptab[2 * a + 1] = r1;
+  }
+  __syncthreads();
+  const int mt = sc.match;
+  const uint32_t one = (uint32_t)(sc.gap_open >> 30) + 1u;  // a 1 the compiler cannot fold
+  const uint32_t ngo2 = (uint32_t)(uint16_t)(-sc.gap_open) * 0x00010001u;
+  const uint32_t nge2 = (uint32_t)(uint16_t)(-sc.gap_extend) * 0x00010001u;
+  int64_t off = 0;
+#pragma unroll
+  for (int c = 0; c < C; c++) off += wl.band_counts[c];
+  int64_t total = wl.band_counts[C];
+  if (off + total > wl.cap) total = wl.cap - off;
+  struct Meta {
+    int64_t p = -1;
+    int S = 0, ie = 0, je = 0;
+    int64_t aoff = 0, boff = 0;
+  };
+  auto load_meta = [&](int64_t idx) {
+    Meta m;
+    if (idx < total) {
+      m.p = wl.bands[off + idx];
+      m.S = rs.score[m.p];
+      m.ie = rs.a_end[m.p];
+      m.je = rs.b_end[m.p];
+      m.aoff = ps.a_off[m.p];
+      m.boff = ps.b_off[m.p];
+    }
+    return m;
+  };
+  const int64_t gstride = (int64_t)gridDim.x * blockDim.x;
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  Meta cur = load_meta(idx);
+  for (; idx < total; idx += gstride) {
+    const Meta nxt = load_meta(idx + gstride);
+    const int64_t p = cur.p;
+    const int S = cur.S;
+    const int ie = cur.ie, je = cur.je;
+    const int M2 = ie + 1, N2 = je + 1;
+    const uint8_t *a = ps.a_code + cur.aoff + ie;  // reversed: a[-i]
+    const uint8_t *b = ps.b_code + cur.boff + je;  // reversed: b[-j]
+    cur = nxt;
+    auto code_at = [&](int j) -> int { return ((unsigned)j < (unsigned)N2 ? (int)b[-j] : kCodePad) | 0x7770; };
+    auto row_code = [&](int r) -> int { return r < M2 ? (int)a[-r] : kCodePad; };
+    auto cap_rows = [&](int t) { t = (t + U - 1) / U * U; return t < M2 ? t : M2; };
+    int t = cap_rows(band_first_cap(S, mt, M2));
+    int fi = -1, fj = -1;
+    bool escalate = false, found = false;
+    uint32_t P[W + 3], Q[W + 3];
+    int cb[NC];
+#pragma unroll
+    for (int d = 0; d < W + 3; d++) {
+      P[d] = 0u;
+      Q[d] = 0xC000C000u;
+    }
+#pragma unroll
+    for (int k = 0; k < NC; k++) cb[k] = code_at(k - G);
+    int a0 = row_code(0), a1 = row_code(1);
+    int i = 0;
+    for (;;) {
+      if (band_gap_bound(t, N2, S, sc) > G) {
+        escalate = true;
+        break;
+      }
+      while (i < t && !found) {
+        const int n0 = row_code(i + U), n1 = row_code(i + U + 1);
+#pragma unroll
+        for (int u = 0; u < U; u += 2) {
+          const int row = i + u;
+          if (!found && row < t) {
+            const int ca = u == 0 ? a0 : row_code(row), cc = u == 0 ? a1 : row_code(row + 1);
+            const uint32_t rm = band_pair16<W, NC>(cb, u, rptab[2 * ca], rptab[2 * ca + 1], rptab[2 * cc],
+                                                   rptab[2 * cc + 1], one, ngo2, nge2, P, Q);
+            if ((int)(rm & 0xffffu) >= S || (int)(rm >> 16) >= S) {
+              // the first cell holding S: row A's cells left to right, then row B's
+              found = true;
+#pragma unroll
+              for (int k = 0; k < W; k++)
+                if (fi < 0 && (int)(P[k] & 0xffffu) == S) {
+                  fi = row;
+                  fj = row - G + k;
+                }
+#pragma unroll
+              for (int k = 2; k < W + 2; k++)
+                if (fi < 0 && (int)(P[k] >> 16) == S) {
+                  fi = row + 1;
+                  fj = row + 1 - G + (k - 2);
+                }
+            }
+          }
+        }
+        if (found || i + U >= M2) break;
+        i += U;
+#pragma unroll
+        for (int k = 0; k < W; k++) cb[k] = cb[k + U];
+#pragma unroll
+        for (int k = W; k < NC; k++) cb[k] = code_at(i - G + k);
+        a0 = n0;
+        a1 = n1;
+      }
+      if (found || t >= M2) break;
+      t = cap_rows(2 * t);
+    }
+    append_agg(wl.wide, wl.wide_count, wl.cap, p, escalate);
+    if (escalate) continue;
+    if (!found || fi < 0 || fi >= M2 || fj < 0 || fj >= N2) {
       rs.flag[p] |= kFlagTooLong;  // inconsistent; reported as an error by the driver
       rs.a_beg[p] = -1;
       rs.b_beg[p] = 0;
@@ -907,8 +1126,13 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
     const int gridb = sms * 8;
     // band classes by half-width 3, 5, 7, 11, 15, 23, 31 (band of 7 .. 63 cells); the
     // segments' counts stay on the device.
-    k_rev_count<<<grid, 256, 0, st>>>(rs, sc, order, ps.n, wl.band_counts);
-    k_rev_scatter<<<grid, 256, 0, st>>>(rs, sc, order, ps.n, wl);
+    // scores s + gO as bytes when no penalty exceeds the gap-open penalty (klign's scorings);
+    // then the packed int16 band kernels take scores up to kBand16Score
+    const bool bi = sc.gap_open > 0 && sc.mismatch <= sc.gap_open && sc.ambiguity <= sc.gap_open &&
+                    sc.match + sc.gap_open <= 255;
+    const int s_cap = bi ? kBand16Score : 0x7fffffff;
+    k_rev_count<<<grid, 256, 0, st>>>(rs, sc, order, ps.n, wl.band_counts, s_cap);
+    k_rev_scatter<<<grid, 256, 0, st>>>(rs, sc, order, ps.n, wl, s_cap);
     // The classes are independent: with side streams they run concurrently, so the
     // latency-bound narrow classes share the SMs with the wide ones.
     cudaStream_t cs[kBandClasses];
@@ -918,17 +1142,14 @@ cudaError_t launch_reverse(int device, const PairSet &ps, const ResultSet &rs, c
       if (e != cudaSuccess) return e;
     }
     for (int c = 0; c < kBandClasses; c++) cs[c] = fan ? fk->side[c] : st;
-    // scores s + gO as bytes when no penalty exceeds the gap-open penalty (klign's scorings)
-    const bool bi = sc.gap_open > 0 && sc.mismatch <= sc.gap_open && sc.ambiguity <= sc.gap_open &&
-                    sc.match + sc.gap_open <= 255;
     if (bi) {
-      k_rev_band<64, 6, true><<<gridb, 128, 0, cs[6]>>>(ps, rs, sc, wl);
-      k_rev_band<48, 5, true><<<gridb, 128, 0, cs[5]>>>(ps, rs, sc, wl);
-      k_rev_band<32, 4, true><<<gridb, 128, 0, cs[4]>>>(ps, rs, sc, wl);
-      k_rev_band<24, 3, true><<<gridb, 128, 0, cs[3]>>>(ps, rs, sc, wl);
-      k_rev_band<16, 2, true><<<gridb, 128, 0, cs[2]>>>(ps, rs, sc, wl);
-      k_rev_band<12, 1, true><<<gridb, 128, 0, cs[1]>>>(ps, rs, sc, wl);
-      k_rev_band<8, 0, true><<<gridb, 128, 0, cs[0]>>>(ps, rs, sc, wl);
+      k_rev_band16<64, 6><<<gridb, 128, 0, cs[6]>>>(ps, rs, sc, wl);
+      k_rev_band16<48, 5><<<gridb, 128, 0, cs[5]>>>(ps, rs, sc, wl);
+      k_rev_band16<32, 4><<<gridb, 128, 0, cs[4]>>>(ps, rs, sc, wl);
+      k_rev_band16<24, 3><<<gridb, 128, 0, cs[3]>>>(ps, rs, sc, wl);
+      k_rev_band16<16, 2><<<gridb, 128, 0, cs[2]>>>(ps, rs, sc, wl);
+      k_rev_band16<12, 1><<<gridb, 128, 0, cs[1]>>>(ps, rs, sc, wl);
+      k_rev_band16<8, 0><<<gridb, 128, 0, cs[0]>>>(ps, rs, sc, wl);
     } else {
       k_rev_band<64, 6, false><<<gridb, 128, 0, cs[6]>>>(ps, rs, sc, wl);
       k_rev_band<48, 5, false><<<gridb, 128, 0, cs[5]>>>(ps, rs, sc, wl);

@@ -5,12 +5,13 @@
 // candidate whether it needs an alignment at all (src/klign.cpp:218-241, :670-739); the
 // aligner's results are then mapped into its Aln records (:260-266, :369-381).  Here all
 // of it runs on the device against a resident contig set:
-//   k_klign_prepare   one thread per candidate: orientation and the mirrored seed
+//   k_klign_prepare   one warp per candidate: orientation and the mirrored seed
 //                     position, the diagonal window clipped to the contig, the oriented
 //                     read written (reverse complement for '-'), the raw-byte perfect-
-//                     match compare; candidates that need an alignment are appended to a
-//                     compacted pair list (window = offset into the resident contig
-//                     codes, no copy) with the batch's longest read and window;
+//                     match compare 32 bytes at a time; candidates that need an
+//                     alignment are appended to a compacted pair list (window = offset
+//                     into the resident contig codes, no copy; one list reservation per
+//                     block and round) with the batch's longest read and window;
 //   alignment         the driver's resident-batch path (forward + begin pass, score2 when
 //                     the driver is in score2 mode) over the compacted list;
 //   k_klign_finish    one thread per candidate: klign's Aln fields from either the

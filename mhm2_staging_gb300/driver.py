@@ -65,6 +65,35 @@ class Timing(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class CallRecord(C.Structure):
+    _fields_ = [(k, C.c_uint64 if k == "seq" else (C.c_int64 if k == "n_pairs" else C.c_double))
+                for k in ("seq", "n_pairs", "copy_in_start", "copy_in_end", "stream_ready", "translated",
+                          "forward_done", "begin_done", "done")]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [
+        ("threads_per_block", C.c_int32),
+        ("blocks_per_sm", C.c_int32),
+        ("lane_rows", C.c_int32),
+        ("wide_try16", C.c_int32),
+        ("last_call_tuned", C.c_int32),
+        ("trials", C.c_int32),
+        ("sample_pairs", C.c_int64),
+        ("tunings", C.c_int64),
+        ("tune_wall_ms", C.c_double),
+        ("trial_ms", C.c_float * 16),
+    ]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "trial_ms"}
+        d["trial_ms"] = [float(x) for x in self.trial_ms[:min(self.trials, 16)]]
+        return d
+
+
 class Limits(C.Structure):
     _fields_ = [("max_b_len", C.c_int32), ("max_coord", C.c_int32), ("int16_ceiling", C.c_int32)]
 
@@ -177,6 +206,9 @@ SIGNATURES: dict[str, tuple] = {
     "mhsw_align_pairs_async": (C.c_int, [_P, C.POINTER(PairsT), _P, C.c_int, C.c_int]),
     "mhsw_align_wait": (C.c_int, [_P]),
     "mhsw_last_timing": (C.c_int, [_P, C.POINTER(Timing)]),
+    "mhsw_last_tuning": (C.c_int, [_P, C.POINTER(Tuning)]),
+    "mhsw_call_history": (C.c_int, [_P, C.POINTER(CallRecord), C.c_int, C.POINTER(C.c_int)]),
+    "mhsw_driver_fix_batch_config": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int]),
     "mhsw_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P), C.c_char_p, C.c_size_t]),
     "mhsw_server_destroy": (None, [_P]),
     "mhsw_server_last_error": (C.c_char_p, [_P]),
@@ -497,13 +529,14 @@ class GPUDriver:
         pt = pairs.c_struct()
         if hints:
             pt.max_a_len, pt.max_b_len, pt.cells, pt.a_bytes, pt.b_bytes = pairs.extents()
-        self._pending = (pairs, out, pt)
+        # the handle keeps up to three calls in flight: their arrays stay referenced here
+        self._pending = (list(getattr(self, "_pending", None) or []) + [(pairs, out, pt)])[-3:]
         self._ck(self._lib.mhsw_align_pairs_async(self._h, C.byref(pt), out.ctypes.data_as(_P) if n else None, 1,
                                                   form), "align_pairs_async")
         return out
 
     def wait(self) -> None:
-        """Completes the batch enqueued by align_pairs_async (mhsw_align_wait)."""
+        """Completes the batches enqueued by align_pairs_async (mhsw_align_wait)."""
         try:
             self._ck(self._lib.mhsw_align_wait(self._h), "align_wait")
         finally:
@@ -532,6 +565,26 @@ class GPUDriver:
     def last_timing(self) -> dict:
         t = Timing()
         self._ck(self._lib.mhsw_last_timing(self._h, C.byref(t)), "last_timing")
+        return t.as_dict()
+
+    def fix_batch_config(self, threads_per_block: int = 0, blocks_per_sm: int = 0, lane_rows: int = 160,
+                         wide_try16: bool = False) -> None:
+        """Fixes the batched form's configuration (tuner off); threads_per_block=0 turns the
+        tuner back on."""
+        self._ck(self._lib.mhsw_driver_fix_batch_config(self._h, threads_per_block, blocks_per_sm, lane_rows,
+                                                        1 if wide_try16 else 0), "fix_batch_config")
+
+    def call_history(self, max_records: int = 64) -> list[dict]:
+        """Device times of the last completed batch calls (mhsw_call_history), oldest first."""
+        buf = (CallRecord * max_records)()
+        k = C.c_int(0)
+        self._ck(self._lib.mhsw_call_history(self._h, buf, max_records, C.byref(k)), "call_history")
+        return [buf[i].as_dict() for i in range(k.value)]
+
+    def last_tuning(self) -> dict:
+        """The batched form's configuration and its last tuning (mhsw_last_tuning)."""
+        t = Tuning()
+        self._ck(self._lib.mhsw_last_tuning(self._h, C.byref(t)), "last_tuning")
         return t.as_dict()
 
 
@@ -573,6 +626,16 @@ class Pairs:
                 raise RuntimeError("Pairs arrays must be contiguous with dtypes uint8/int64/int32")
         return PairsT(self.a_seq.ctypes.data, self.a_off.ctypes.data, self.a_len.ctypes.data,
                       self.b_seq.ctypes.data, self.b_off.ctypes.data, self.b_len.ctypes.data, self.n, 0, 0, 0.0, 0, 0)
+
+    def write_file(self, path) -> None:
+        """The batch as a pair file (little-endian int64 n, A bytes, B bytes; the two byte
+        arenas; int64 A and B offsets; int32 A and B lengths), the input of the C++
+        drop-in block benchmark (klign_block_bench)."""
+        with open(path, "wb") as f:
+            f.write(np.array([self.n, self.a_seq.nbytes, self.b_seq.nbytes], dtype="<i8").tobytes())
+            for arr, dt in ((self.a_seq, "u1"), (self.b_seq, "u1"), (self.a_off, "<i8"), (self.b_off, "<i8"),
+                            (self.a_len, "<i4"), (self.b_len, "<i4")):
+                f.write(np.ascontiguousarray(arr, dtype=dt).tobytes())
 
     def a(self, i: int) -> bytes:
         o = int(self.a_off[i])

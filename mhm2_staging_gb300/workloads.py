@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+from pathlib import Path
 
 import numpy as np
 
@@ -20,13 +21,12 @@ from . import build as _build
 from .driver import Pairs
 
 CONFIG_PAIRS = {0: 10_000, 1: 1_000_000, 2: 4_000_000, 4: 200_000}
-_GEN = None
+_GEN: dict = {}
 
 
-def _gen() -> C.CDLL:
-    global _GEN
-    if _GEN is None:
-        p = _build.gen_lib_path()
+def _gen(path=None) -> C.CDLL:
+    p = Path(path) if path else _build.gen_lib_path()
+    if p not in _GEN:
         if not p.exists():
             raise RuntimeError(f"{p} missing: run mhm2_staging_gb300.build.build()")
         g = C.CDLL(str(p))
@@ -40,16 +40,17 @@ def _gen() -> C.CDLL:
         g.mhsw_gen_count.argtypes = [C.c_void_p]
         g.mhsw_gen_free.restype = None
         g.mhsw_gen_free.argtypes = [C.c_void_p]
-        _GEN = g
-    return _GEN
+        _GEN[p] = g
+    return _GEN[p]
 
 
 def generate(config: int, n: int | None = None, seed: int | None = None, first: int = 0,
-             threads: int | None = None) -> Pairs:
-    """Pairs [first, first+n) of `config` (seed defaults to the config number)."""
+             threads: int | None = None, gen_lib=None) -> Pairs:
+    """Pairs [first, first+n) of `config` (seed defaults to the config number).  gen_lib
+    names another build of the generator library (the same source)."""
     if config not in CONFIG_PAIRS:
         raise ValueError(f"unknown config {config}")
-    g = _gen()
+    g = _gen(gen_lib)
     n = CONFIG_PAIRS[config] if n is None else n
     seed = config if seed is None else seed
     threads = threads or min(32, os.cpu_count() or 4)

@@ -28,6 +28,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "liboracle.so"
+GEN_SO = HERE / "_build" / "libmhsw_gen.so"
 REF_SO = HERE / "_ref" / "libssw_ref.so"
 REF_SHIM_SO = HERE / "_ref" / "libssw_ref_shim.so"
 STAGED_SSW = HERE / "_ref" / "ssw_src"
@@ -43,7 +44,7 @@ def build(with_reference: bool | None = None) -> None:
     container): libssw_ref.so (SSE2), its shim twin libssw_ref_shim.so, the staged copy of
     the SSW sources for the aarch64 host, and the ADEPT comparator cubin.  On aarch64 with
     the staged sources: libssw_ref.so through the NEON shim."""
-    subprocess.run(["make", "-s", "-C", str(HERE), "_build/liboracle.so"], check=True)
+    subprocess.run(["make", "-s", "-C", str(HERE), "_build/liboracle.so", "_build/libmhsw_gen.so"], check=True)
     if with_reference is False:
         return
     ref = f"REF={REFERENCE_ROOT}"

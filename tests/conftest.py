@@ -13,6 +13,16 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+def pytest_collection_modifyitems(config, items):
+    """GPU tests get a 10-minute limit where pytest-timeout is installed (the thread method
+    ends the process, so a test stuck in a host wait cannot hold the GPU for longer)."""
+    if not config.pluginmanager.hasplugin("timeout"):
+        return
+    for item in items:
+        if item.get_closest_marker("gpu") and not item.get_closest_marker("timeout"):
+            item.add_marker(pytest.mark.timeout(600, method="thread"))
+
+
 @pytest.fixture(scope="session")
 def built():
     """Builds libmhsw.so / libmhsw_gen.so / liboracle.so once per session."""

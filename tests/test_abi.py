@@ -63,6 +63,20 @@ def test_host_side_status_codes(lib):
         lib.mhsw_driver_destroy(h)
 
 
+def test_tuning_record_of_a_fresh_handle(lib):
+    """A handle that never ran the batched form reports the default configuration."""
+    h = C.c_void_p()
+    assert lib.mhsw_driver_create(C.byref(h)) == 0
+    try:
+        t = D.Tuning()
+        assert lib.mhsw_last_tuning(h, C.byref(t)) == 0
+        assert (t.threads_per_block, t.blocks_per_sm, t.lane_rows, t.wide_try16) == (128, 0, 160, 0)
+        assert (t.tunings, t.trials, t.last_call_tuned) == (0, 0, 0)
+        assert lib.mhsw_last_tuning(h, None) == 2  # MHSW_ERR_ARG
+    finally:
+        lib.mhsw_driver_destroy(h)
+
+
 def test_cigar_format_and_state_checks(lib):
     """mhsw_cigar_format is host code: SAM text of BAM-encoded ops (Alignment::cigar_string)."""
     ops = (C.c_uint32 * 5)((3 << 4) | 4, (8 << 4) | 7, (1 << 4) | 8, (12 << 4) | 1, (150 << 4) | 2)

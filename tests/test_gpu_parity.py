@@ -28,12 +28,25 @@ def test_config0_all_pairs(gpu, form):
     assert not _diff(got, want, pairs)
 
 
-@pytest.mark.parametrize("cfg,n", [(1, 20000), (2, 20000), (4, 2000)])
+_SAMPLES: dict = {}
+
+
+def _sample(cfg: int, n: int):
+    """Pairs and oracle results of a workload sample, computed once for both forms (the
+    long-reference sample through the oracle's vectorised form, bit-exact with the scalar
+    one: tests/test_oracle.py)."""
+    if (cfg, n) not in _SAMPLES:
+        pairs = workloads.generate(cfg, n=n)
+        want = oracle.align_batch_lanes(pairs, SC) if cfg == 4 else oracle.align_batch(pairs, SC)
+        _SAMPLES[(cfg, n)] = (pairs, want)
+    return _SAMPLES[(cfg, n)]
+
+
+@pytest.mark.parametrize("cfg,n", [(1, 20000), (2, 20000), (4, 20000)])
 @pytest.mark.parametrize("form", [FORM_PLAIN, FORM_BATCHED])
 def test_config_samples(gpu, cfg, n, form):
-    pairs = workloads.generate(cfg, n=n)
+    pairs, want = _sample(cfg, n)
     got = gpu.align_pairs(pairs, form=form)
-    want = oracle.align_batch(pairs, SC)
     assert not _diff(got, want, pairs)
 
 
@@ -279,8 +292,9 @@ def test_async_halves_alternating_handles(built):
 
 
 def test_async_calls_in_flight_on_one_handle(built):
-    """Several host batches enqueued back to back on one handle (two in flight, the
-    copies of one overlapping the other's kernels): every result matches the oracle."""
+    """Several host batches enqueued back to back on one handle (three in flight, the
+    copies of later ones overlapping earlier ones' kernels): every result matches the
+    oracle."""
     batches = [workloads.generate(cfg, n=n, first=300 + k) for k, (cfg, n) in
                enumerate([(2, 30000), (1, 10000), (2, 30000), (0, 10000), (2, 5000), (1, 1)])]
     d = GPUDriver()

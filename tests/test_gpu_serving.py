@@ -128,3 +128,29 @@ def test_bad_requests_are_rejected(contigs, requests):
     with pytest.raises(RuntimeError, match="status 2"):
         srv.submit(bad)
     srv.close()
+
+
+def test_full_size_contig_set_with_concurrent_batches(built):
+    """The serving workload's own contig set (200 MB, lognormal lengths up to 200 kb)
+    resident on the device; request batches of 1k..64k submitted together from several
+    threads (their micro-batches overlap on the device), every result bit-exact against
+    the oracle on the same (read, window) pairs."""
+    big = S.generate_contigs(200 << 20, seed=3)
+    req = S.generate_requests(big, 60000, seed=11)
+    srv = S.Server(slots=3, max_pairs_per_batch=65536)
+    srv.load_contigs(big)
+    cuts = [0, 1024, 9000, 42000, 60000]
+    out = [None] * (len(cuts) - 1)
+
+    def one(k):
+        out[k] = srv.wait(srv.submit(req.slice(cuts[k], cuts[k + 1])))
+
+    th = [threading.Thread(target=one, args=(k,)) for k in range(len(cuts) - 1)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    out5 = np.concatenate([o[0] for o in out])
+    want, _ = _want(big, req)
+    assert not _diff(out5, want)
+    srv.close()

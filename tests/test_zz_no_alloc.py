@@ -1,8 +1,8 @@
 """The allocation-free forward entry point, mhsw_forward_noalloc, through the C ABI.
 
 Compared with the driver's entry point (mhsw_align_pairs: score, a_end and b_end are
-columns 0, 2 and 4 of its result) on the same device-resident batch, on two calls in a
-row, so the second call runs on scratch the first one left behind.
+columns 0, 2 and 4 of its result) and with the oracle on the same device-resident batch,
+on two calls in a row, so the second call runs on scratch the first one left behind.
 """
 import ctypes as C
 
@@ -34,6 +34,56 @@ def _upload(pairs: Pairs, torch):
     dp = D.DevicePairs(*(t.data_ptr() for t in tens), n=pairs.n, max_a_len=int(pairs.a_len.max()),
                        max_b_len=int(pairs.b_len.max()))
     return dp, tens
+
+
+def _run_twice(pairs: Pairs, want: np.ndarray, torch, max_a: int | None = None, max_b: int | None = None):
+    dp, keep = _upload(pairs, torch)
+    if max_a:
+        dp.max_a_len, dp.max_b_len = max_a, max_b
+    out3 = torch.full((pairs.n, 3), -7, dtype=torch.int32, device="cuda:0")
+    for call in range(2):
+        out3.fill_(-7)
+        torch.cuda.synchronize()
+        D.forward_noalloc(dp, out3.data_ptr(), SCORES)
+        torch.cuda.synchronize()
+        got = out3.cpu().numpy()
+        bad = np.nonzero((got != want).any(axis=1))[0]
+        assert len(bad) == 0, (f"call {call}: {len(bad)} of {pairs.n} differ; first {int(bad[0])}: "
+                               f"noalloc={got[bad[0]].tolist()} want={want[bad[0]].tolist()}")
+    del keep
+
+
+def test_noalloc_matches_oracle_twice(gpu):
+    from oracle import oracle
+
+    torch = pytest.importorskip("torch")
+    pairs = _batch()
+    _run_twice(pairs, oracle.align_batch(pairs, tuple(abs(x) for x in SCORES))[:, [0, 2, 4]], torch)
+
+
+def test_noalloc_scratch_reused_within_a_call(gpu):
+    """Stated maxima far above the pairs' own lengths (500,000 A, 60,000 B bytes) leave
+    room in the scratch array for only a few dozen lane groups, so each group aligns many
+    pairs of a call one after another on its own share: mixed lengths, A of several
+    strips, B of tens of thousands of bases.  (The entry point's limits leave room for at
+    least 19 groups, so a block never has fewer than its 8 groups.)"""
+    from oracle import oracle
+
+    torch = pytest.importorskip("torch")
+    parts = [workloads.generate(2, n=1500, first=77), workloads.generate(1, n=400, first=9)]
+    a = [p.a(i) for p in parts for i in range(p.n)]
+    b = [p.b(i) for p in parts for i in range(p.n)]
+    rng = np.random.default_rng(5)
+    def bases(k: int) -> bytes:
+        return np.frombuffer(b"ACGT", dtype=np.uint8)[rng.integers(0, 4, k)].tobytes()
+
+    for la, lb in ((300, 50000), (2000, 20000), (5000, 6000), (130, 59000)):
+        read = bases(la)
+        a.append(read)
+        b.append(bases(lb // 2) + read + bases(max(lb - lb // 2 - la, 10)))
+    pairs = Pairs.from_lists(a, b)
+    want = oracle.align_batch(pairs, tuple(abs(x) for x in SCORES))[:, [0, 2, 4]]
+    _run_twice(pairs, want, torch, max_a=500_000, max_b=60_000)
 
 
 def test_noalloc_matches_align_pairs_twice(gpu):
