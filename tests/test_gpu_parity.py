@@ -139,6 +139,35 @@ def test_long_a_strips(built):
     assert not _diff(got, want, pairs)
 
 
+@pytest.mark.parametrize("form", [FORM_PLAIN, FORM_BATCHED])
+def test_scores_at_the_packed_begin_cap(built, form):
+    """Identical and near-identical pairs whose scores lie just below, at and above 16,000,
+    the largest score the packed int16 begin bands take: at or below it the begin search
+    runs in a packed band (values up to the score plus gap-open and match inside int16),
+    above it in the int32 wavefront."""
+    import random
+
+    rng = random.Random(16000)
+    a, b = [], []
+    for n, subs in ((15990, 0), (16000, 0), (16001, 0), (16010, 1), (16012, 2)):
+        x = "".join(rng.choice("ACGT") for _ in range(n))
+        y = list(x)
+        for _ in range(subs):
+            k = rng.randrange(2000, n - 2000)
+            y[k] = rng.choice([c for c in "ACGT" if c != y[k]])
+        flank = "".join(rng.choice("ACGT") for _ in range(37))
+        a.append(x)
+        b.append(flank + "".join(y) + flank)
+    pairs = Pairs.from_lists(a, b)
+    want = oracle.align_batch(pairs, SC, 5)
+    assert sorted(want[:, 0].tolist())[0] < 16000 and want[:, 0].max() > 16000 and 16000 in want[:, 0]
+    d = GPUDriver()
+    d.init(0, 1, 1, -3, -5, -2, 0)
+    d.set_ambiguity(-2)
+    got = d.align_pairs(pairs, form=form)
+    assert not _diff(got, want, pairs)
+
+
 def test_high_scores_long_near_identical_pairs(built):
     """Near-identical 20,000-base pairs with about 20 substitutions and an indel: scores
     above 16,000 whose gap bound exceeds the widest begin band, so the begin search takes
