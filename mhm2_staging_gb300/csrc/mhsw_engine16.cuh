@@ -31,6 +31,8 @@
 //     loop is unrolled by two so the two word sets alternate registers).
 //  4. B codes are read from global memory (each loaded two steps before its use) instead
 //     of being staged in shared memory, so a group's shared memory is its profile table only.
+//     The sweep runs in three phases: the middle one, where every lane's look-ahead column
+//     lies inside B, loads codes without the bounds test and the N substitution.
 //
 // Score2 mode (S2) also produces what SSW's second-best score is computed from
 // (ssw_core.cpp:489, :513-536): each A row's maximum of H, over B extended to P columns
@@ -40,6 +42,8 @@
 // unchanged.  The profile table then has a sixth code (zero score), and each row keeps a
 // running maximum over the valid columns (one DPX add-max per row and step).
 #pragma once
+#include <type_traits>
+
 #include "mhsw_engine.cuh"
 
 namespace mhsw {
@@ -91,6 +95,14 @@ __device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c) 
   return r;
 }
 
+// PRMT with a selector held in a register; unlike __byte_perm (which reads only the low
+// three bits of each selector nibble) it keeps the sign-replicate bit.
+__device__ __forceinline__ uint32_t prmt_sel(uint32_t a, uint32_t b, uint32_t sel) {
+  uint32_t r;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+  return r;
+}
+
 __device__ __forceinline__ uint32_t sign_mask16(uint32_t x) {
   // each 16-bit half -> 0xffff if its bit 15 is set, else 0 (PRMT sign-replicate mode)
   uint32_t r;
@@ -115,13 +127,13 @@ struct Step16 {
   static constexpr uint32_t kKeyMask = KeyBits<K>::kMask;
   // S2: Rm[k] keeps each row's running maximum over valid columns; vmask is 0 in a half
   // whose column is valid at this step and -16384 otherwise (an add-max then ignores it).
-  __device__ static __forceinline__ void run(int t, uint32_t z, const uint32_t (&Wlo)[K],
+  __device__ static __forceinline__ void run(int t, uint32_t zH, uint32_t zE, uint32_t sel, const uint32_t (&Wlo)[K],
                                              const uint32_t (&Phi)[K], uint32_t (&H)[K], uint32_t (&F)[K],
-                                             uint32_t &Hlast, uint32_t &Ecout, uint32_t &HtopPrev, uint32_t &Zout,
+                                             uint32_t &Hlast, uint32_t &Ecout, uint32_t &HtopPrev,
                                              uint32_t &Kl, uint32_t &Jp, uint32_t NGE, uint32_t NGO, uint32_t one,
                                              uint32_t eight, uint32_t (&Rm)[K], uint32_t vmask) {
-    uint32_t Ev = __byte_perm(z, Ecout, 0x5432);  // lo: from the left lane, hi: own lo half
-    const uint32_t Htop = __byte_perm(z, Hlast, 0x5410);
+    uint32_t Ev = prmt_sel(zE, Ecout, sel);  // lo: from the left lane, hi: own lo half
+    const uint32_t Htop = prmt_sel(zH, Hlast, sel);
     uint32_t Hd = HtopPrev;
     HtopPrev = Htop;
     uint32_t key[K];
@@ -143,7 +155,6 @@ struct Step16 {
     uint32_t Kn = Kl;
 #pragma unroll
     for (int k = 0; k < K; k += 2) Kn = __vimax3_s16x2(Kn, key[k], key[k + 1]);
-    Zout = __byte_perm(H[K - 1], Ev, 0x7632);
     Hlast = H[K - 1];
     Ecout = Ev;
     // record the step where the running key strictly grows
@@ -203,7 +214,6 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
   const int NP = S2 ? rmo.P : N;  // columns swept ([N, NP) score 0 in score2 mode)
   const int T_end = NP + 2 * G - 1;
   const uint4 *tab = reinterpret_cast<const uint4 *>(gs.prof);
-  const uint32_t zmask = lane == 0 ? 0u : 0xffffffffu;  // lane 0 sees the zero top boundary
   // 1 and 2^KB as values the compiler cannot fold (gs.pad is a launch argument >= 0)
   const uint32_t one = (uint32_t)(gs.pad >> 30) + 1u;
   const uint32_t scale = one << KB;
@@ -230,6 +240,8 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
     }
     __syncwarp(gmask);
 
+    const bool first_strip = (s == 0);
+    const bool last_strip = (s == nstrips - 1);
     uint32_t H[K], F[K], Wlo[K], HA[K], HB[K];
 #pragma unroll
     for (int k = 0; k < K; k++) {
@@ -239,14 +251,14 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
 #pragma unroll
     for (int w = 0; w < K; w++) HB[w] = 0u;  // hi words before column 0 (biased 0)
     uint32_t Hlast = 0u, Ecout = 0u, HtopPrev = 0u;
-    uint32_t Zout = 0u;  // (lo: H of the hi-last row, hi: E^ below it)
+    // lane 0 of the first strip reads zeros above: the selector replicates the sign of a
+    // top byte of its own (non-negative) H and E^ words; other lanes take the left lane's hi halves
+    const uint32_t sel = (lane == 0 && first_strip) ? 0x54BBu : 0x5432u;
     uint32_t Kl = 0u;    // running key per half
     uint32_t Jp = 0u;    // step of the last strict increase of Kl, per half
     uint32_t Rm[K];      // score2 mode: running row maxima over valid columns
 #pragma unroll
     for (int k = 0; k < K; k++) Rm[k] = 0u;
-    const bool first_strip = (s == 0);
-    const bool last_strip = (s == nstrips - 1);
     const int j0 = -2 * lane;  // lo column at step 0
     auto code_at = [&](int j) -> int {
       if ((unsigned)j < (unsigned)N) return (int)bg[j];
@@ -263,39 +275,66 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
     // codes of the even and odd steps, each loaded two steps before its use
     int ceven = code_at(j0), codd = code_at(j0 + 1);
 
-    auto top = [&](int t, uint32_t zs) -> uint32_t {
-      uint32_t z = zs & zmask;
-      if (MULTI && lane == 0 && !first_strip && t < NP) z = bnd[t];
-      return z;
+    // the left lane's H of its hi-last row and E^ below it (hi halves); lane 0 of a later
+    // strip reads them from the boundary row (lo: H, hi: E^), zero past column NP
+    auto top = [&](int t, uint32_t &zH, uint32_t &zE) {
+      zH = __shfl_up_sync(gmask, Hlast, 1, G);
+      zE = __shfl_up_sync(gmask, Ecout, 1, G);
+      if (MULTI && lane == 0 && !first_strip) {
+        const uint32_t b = t < NP ? bnd[t] : 0u;
+        zH = __byte_perm(b, 0u, 0x1000);
+        zE = b;
+      }
     };
     auto out_bnd = [&](int t) {
       if (MULTI && !last_strip && lane == G - 1) {
         const int jh = t - 2 * lane - 1;  // hi-half column of the last lane
-        if (jh >= 0 && jh < NP) bnd[jh] = Zout;
+        if (jh >= 0 && jh < NP) bnd[jh] = __byte_perm(Hlast, Ecout, 0x7632);
       }
     };
     int t = 0;
-    for (; t + 1 < T_end; t += 2) {
+    const uint8_t *bl = bg + j0;
+    // Two steps; `guarded` (std::true_type / std::false_type) says whether the look-ahead
+    // codes need the bounds test.
+    auto two_steps = [&](auto guarded) {
+      constexpr bool kGuard = decltype(guarded)::value;
       // even step: hi words into HA; the high half uses HB (previous column)
       int c = ceven;
-      ceven = code_at(t + 2 + j0);
+      ceven = kGuard ? code_at(t + 2 + j0) : (int)bl[t + 2];
       ST::load(tab, c, lane, Wlo, HA);
-      uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
-      ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale, Rm, vmask_at(t));
+      uint32_t zH, zE;
+      top(t, zH, zE);
+      ST::run(t, zH, zE, sel, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Kl, Jp, NGE, NGO, one, scale, Rm, vmask_at(t));
       out_bnd(t);
       // odd step: hi words into HB; the high half uses HA
       c = codd;
-      codd = code_at(t + 3 + j0);
+      codd = kGuard ? code_at(t + 3 + j0) : (int)bl[t + 3];
       ST::load(tab, c, lane, Wlo, HB);
-      z = top(t + 1, __shfl_up_sync(gmask, Zout, 1, G));
-      ST::run(t + 1, z, Wlo, HA, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale, Rm,
+      top(t + 1, zH, zE);
+      ST::run(t + 1, zH, zE, sel, Wlo, HA, H, F, Hlast, Ecout, HtopPrev, Kl, Jp, NGE, NGO, one, scale, Rm,
               vmask_at(t + 1));
       out_bnd(t + 1);
+    };
+    // The look-ahead columns t+2+j0 and t+3+j0 lie in [0, N) for every lane of the group
+    // (j0 = -2 lane, lane < G) when 2G-4 <= t <= N-4.
+    const int tm0 = 2 * G - 4, tm1 = N - 3;
+    for (; t + 1 < T_end && t < tm0; t += 2) two_steps(std::true_type{});
+    // eight steps per iteration in the middle phase (the loop's own instructions and the
+    // register moves at its back edge are paid once per eight steps)
+    for (; t + 6 < tm1;) {
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        two_steps(std::false_type{});
+        t += 2;
+      }
     }
+    for (; t < tm1; t += 2) two_steps(std::false_type{});
+    for (; t + 1 < T_end; t += 2) two_steps(std::true_type{});
     if (t < T_end) {
       ST::load(tab, ceven, lane, Wlo, HA);
-      const uint32_t z = top(t, __shfl_up_sync(gmask, Zout, 1, G));
-      ST::run(t, z, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Zout, Kl, Jp, NGE, NGO, one, scale, Rm, vmask_at(t));
+      uint32_t zH, zE;
+      top(t, zH, zE);
+      ST::run(t, zH, zE, sel, Wlo, HB, H, F, Hlast, Ecout, HtopPrev, Kl, Jp, NGE, NGO, one, scale, Rm, vmask_at(t));
       out_bnd(t);
     }
 

@@ -107,6 +107,41 @@ def test_random_scorings(built, seed):
         assert not _diff(got, want, pairs), (sc, form)
 
 
+def _embedded_reads(seed: int, n: int, lo: int, hi: int) -> Pairs:
+    """Reads of lo..hi bases with 2% substitutions, each inside a window of up to 120
+    random flanking bases: the score climbs from the first rows on."""
+    rng = np.random.default_rng(seed)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    a, b = [], []
+    for _ in range(n):
+        read = acgt[rng.integers(0, 4, int(rng.integers(lo, hi + 1)))]
+        mut = read.copy()
+        sub = rng.random(len(read)) < 0.02
+        mut[sub] = acgt[rng.integers(0, 4, int(sub.sum()))]
+        left = acgt[rng.integers(0, 4, int(rng.integers(0, 120)))]
+        right = acgt[rng.integers(0, 4, int(rng.integers(0, 120)))]
+        a.append(read.tobytes().decode())
+        b.append(np.concatenate([left, mut, right]).tobytes().decode())
+    return Pairs.from_lists(a, b)
+
+
+@pytest.mark.parametrize("match", [16, 40, 63])
+def test_high_match_scorings(built, match):
+    """Match scores of 16-63 take H above 255 within the first lane's rows of every lane
+    group size and row count per lane (reads of 24-260 bases), on the keyed int16 engine
+    where the score bound fits its keys and on the int32 engine (or the int16 try and its
+    re-run) where it does not; both forms against the oracle."""
+    sc = (match, 4, 6, 1, 2)
+    d = GPUDriver()
+    d.init(0, 1, match, -4, -6, -1, 0)
+    d.set_ambiguity(-2)
+    pairs = _embedded_reads(match, 1500, 24, 260)
+    want = oracle.align_batch(pairs, sc)
+    for form in (FORM_PLAIN, FORM_BATCHED):
+        got = d.align_pairs(pairs, form=form)
+        assert not _diff(got, want, pairs), (sc, form)
+
+
 def test_forced_int32_rerun(built):
     d = GPUDriver()
     d.init(0, 1, 1, -3, -5, -2, 300)
