@@ -845,6 +845,11 @@ int copy_batch_in(mhsw_driver *d, mhsw_driver::InSet &in, const mhsw_pairs *pair
   for (int k = 0; k < kLanes; k++) {
     if (after_free) {
       if (in.used) MHSW_CK(cudaStreamWaitEvent(d->copy_st[k], in.free_ev, 0), "wait input set");
+      // calls copy in one after another: the first of several calls enqueued together
+      // then gets the whole copy bandwidth instead of sharing it, and its kernels start
+      // as early as they can (the later calls' copies still run under its kernels)
+      for (int m = 0; m < kLanes; m++)
+        if (m != k) MHSW_CK(cudaStreamWaitEvent(d->copy_st[k], d->copy_ev[m], 0), "wait previous copies");
     } else {
       MHSW_CK(cudaStreamWaitEvent(d->copy_st[k], d->copy_ev[0], 0), "wait stream");
     }

@@ -171,10 +171,12 @@ __global__ void __launch_bounds__(256) k_fwd16(PairSet ps, ResultSet rs, Scoring
 }
 
 // Begin pass, banded.  Each pair's search is first assigned a band class: the
-// narrowest instantiation whose half-width holds the gap bound at the first row cap
-// (k_rev_count / k_rev_scatter group the pairs into one segment per class), so every
-// thread of a class kernel has a pair to work on.  One thread per pair: the band is WB-1
-// cells wide (half-width G = WB/2 - 1) and lives in registers, fully unrolled; the codes
+// narrowest instantiation whose width holds the alignment's largest drift to each side
+// of the end cell's diagonal at the first row cap (band_sides: vertical gaps also cost
+// rows, so that side's bound is the tighter one; the band sits asymmetrically around the
+// diagonal) (k_rev_count / k_rev_scatter group the pairs into one segment per class), so
+// every thread of a class kernel has a pair to work on.  One thread per pair: the band is
+// WB-1 = 2G+1 cells wide and lives in registers, fully unrolled; the codes
 // of a row's band are loaded before its dependency chain starts.  Rows whose band lies
 // inside [0, N2) run without bound checks.  The row cap t starts at 2*score/match + 16
 // and doubles until a row reaches the score, so short low-score alignments stay in a
@@ -207,6 +209,52 @@ __host__ __device__ __forceinline__ int band_gap_bound(int t, int N2, int S, con
   return gap_cells_bound(t < N2 ? t : N2, S, sc);
 }
 
+// How far such an alignment can drift from the end cell's diagonal to either side.  I
+// vertical gap cells (a row each, no column) leave at most t - I diagonal steps:
+// S <= (t - I)*match - I*gmin - c, c = max(gO - gE, 0) once, so
+// I <= (t*match - S - c) / (match + gmin); likewise J horizontal gap cells leave at most
+// N2 - J, so J <= (N2*match - S - c) / (match + gmin).  Both are at most the total g.  A
+// band over columns [row - L, row - L + W) holds every such alignment when I <= L and
+// J <= W - 1 - L.
+__host__ __device__ __forceinline__ void band_sides(int t, int N2, int S, const Scoring &sc, int &I, int &J) {
+  const int g = band_gap_bound(t, N2, S, sc);
+  const int gmin = sc.gap_open < sc.gap_extend ? sc.gap_open : sc.gap_extend;
+  const int mg = sc.match + (gmin > 0 ? gmin : 1);
+  const int c = sc.gap_open > sc.gap_extend ? sc.gap_open - sc.gap_extend : 0;
+  const int st = t * sc.match - S - c, sn = N2 * sc.match - S - c;
+  I = st < mg ? 0 : st / mg;
+  J = sn < mg ? 0 : sn / mg;
+  if (I > g) I = g;
+  if (J > g) J = g;
+}
+
+// The narrowest band class whose width holds both sides at the first row cap
+// (kBandClasses: none does).
+__host__ __device__ __forceinline__ int band_fit(int S, int M2, int N2, const Scoring &sc) {
+  int I, J;
+  band_sides(band_first_cap(S, sc.match, M2), N2, S, sc, I, J);
+  int c = kBandClasses;
+#pragma unroll
+  for (int k = kBandClasses - 1; k >= 0; k--)
+    if (I + J <= 2 * band_half(k)) c = k;
+  return c;
+}
+
+// The band's left extent for a pair of class half-width G: its vertical bound at the first
+// row cap, with the room the class leaves beyond both bounds split between the sides.
+__device__ __forceinline__ int band_left(int S, int M2, int N2, const Scoring &sc, int G) {
+  int I, J;
+  band_sides(band_first_cap(S, sc.match, M2), N2, S, sc, I, J);
+  return I + (2 * G - I - J) / 2;
+}
+
+// True when an alignment reaching S within t rows may leave the band [row - L, row - L + 2G].
+__device__ __forceinline__ bool band_outgrown(int t, int N2, int S, const Scoring &sc, int L, int G) {
+  int I, J;
+  band_sides(t, N2, S, sc, I, J);
+  return I > L || J > 2 * G - L;
+}
+
 // Band class of pair p (0 .. kBandClasses-1), kBandClasses for the wavefront, or -1 when
 // there is nothing to search (score 0, or a pair the forward pass rejected); those get
 // their begin written here.
@@ -220,12 +268,7 @@ __device__ __forceinline__ int band_class(const ResultSet &rs, const Scoring &sc
     return -1;
   }
   if (S > s_cap) return kBandClasses;
-  const int M2 = rs.a_end[p] + 1, N2 = rs.b_end[p] + 1;
-  const int g = band_gap_bound(band_first_cap(S, sc.match, M2), N2, S, sc);
-#pragma unroll
-  for (int c = 0; c < kBandClasses; c++)
-    if (g <= band_half(c)) return c;
-  return kBandClasses;
+  return band_fit(S, rs.a_end[p] + 1, rs.b_end[p] + 1, sc);
 }
 
 // Warp-aggregated append of p to list[*count] (one atomic per distinct counter).
@@ -276,14 +319,7 @@ __global__ void __launch_bounds__(256) k_rev_scatter(ResultSet rs, Scoring sc, c
     const int S = rs.score[p];
     int c = -1;
     if (!((rs.flag[p] & kFlagTooLong) || S <= 0)) {
-      const int M2 = rs.a_end[p] + 1, N2 = rs.b_end[p] + 1;
-      const int g = band_gap_bound(band_first_cap(S, sc.match, M2), N2, S, sc);
-      c = kBandClasses;
-      if (S <= s_cap) {
-#pragma unroll
-        for (int k = kBandClasses - 1; k >= 0; k--)
-          if (g <= band_half(k)) c = k;
-      }
+      c = S <= s_cap ? band_fit(S, rs.a_end[p] + 1, rs.b_end[p] + 1, sc) : kBandClasses;
     }
     // one append per class present in the warp: lanes of a class share one atomic
     const unsigned act = __activemask();
@@ -459,6 +495,7 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
     // row caps are kept at multiples of U (or M2) so the window always slides by U
     auto cap_rows = [&](int t) { t = (t + U - 1) / U * U; return t < M2 ? t : M2; };
     int t = cap_rows(band_first_cap(S, mt, M2));
+    const int L = band_left(S, M2, N2, sc, G);  // row i's band: columns i - L + [0, W)
     int fi = -1, fj = -1;
     bool escalate = false, found = false;
     int H[W + 1], E[W + 1], cb[NC];
@@ -468,11 +505,11 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
       E[d] = NEG;
     }
 #pragma unroll
-    for (int k = 0; k < NC; k++) cb[k] = code_at(k - G);
+    for (int k = 0; k < NC; k++) cb[k] = code_at(k - L);
     int a0 = row_code(0), a1 = row_code(1);  // the block's first row pair
-    int i = 0;  // first row of the current block; the window covers columns i - G + [0, NC)
+    int i = 0;  // first row of the current block; the window covers columns i - L + [0, NC)
     for (;;) {
-      if (band_gap_bound(t, N2, S, sc) > G) {
+      if (band_outgrown(t, N2, S, sc, L, G)) {
         escalate = true;
         break;
       }
@@ -491,7 +528,7 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
             if ((km >> 7) >= S) {
               found = true;
               fi = row + 1 - ((km >> 6) & 1);
-              fj = fi - G + (63 - (km & 63));
+              fj = fi - L + (63 - (km & 63));
             }
           }
         }
@@ -500,7 +537,7 @@ __global__ void __launch_bounds__(128) k_rev_band(PairSet ps, ResultSet rs, Scor
 #pragma unroll
         for (int k = 0; k < W; k++) cb[k] = cb[k + U];
 #pragma unroll
-        for (int k = W; k < NC; k++) cb[k] = code_at(i - G + k);
+        for (int k = W; k < NC; k++) cb[k] = code_at(i - L + k);
         a0 = n0;
         a1 = n1;
       }
@@ -633,6 +670,7 @@ __global__ void __launch_bounds__(128) k_rev_band16(PairSet ps, ResultSet rs, Sc
     auto row_code = [&](int r) -> int { return r < M2 ? (int)a[-r] : kCodePad; };
     auto cap_rows = [&](int t) { t = (t + U - 1) / U * U; return t < M2 ? t : M2; };
     int t = cap_rows(band_first_cap(S, mt, M2));
+    const int L = band_left(S, M2, N2, sc, G);  // row i's band: columns i - L + [0, W)
     int fi = -1, fj = -1;
     bool escalate = false, found = false;
     uint32_t P[W + 3], Q[W + 3];
@@ -643,11 +681,11 @@ __global__ void __launch_bounds__(128) k_rev_band16(PairSet ps, ResultSet rs, Sc
       Q[d] = 0xC000C000u;
     }
 #pragma unroll
-    for (int k = 0; k < NC; k++) cb[k] = code_at(k - G);
+    for (int k = 0; k < NC; k++) cb[k] = code_at(k - L);
     int a0 = row_code(0), a1 = row_code(1);
     int i = 0;
     for (;;) {
-      if (band_gap_bound(t, N2, S, sc) > G) {
+      if (band_outgrown(t, N2, S, sc, L, G)) {
         escalate = true;
         break;
       }
@@ -667,13 +705,13 @@ __global__ void __launch_bounds__(128) k_rev_band16(PairSet ps, ResultSet rs, Sc
               for (int k = 0; k < W; k++)
                 if (fi < 0 && (int)(P[k] & 0xffffu) == S) {
                   fi = row;
-                  fj = row - G + k;
+                  fj = row - L + k;
                 }
 #pragma unroll
               for (int k = 2; k < W + 2; k++)
                 if (fi < 0 && (int)(P[k] >> 16) == S) {
                   fi = row + 1;
-                  fj = row + 1 - G + (k - 2);
+                  fj = row + 1 - L + (k - 2);
                 }
             }
           }
@@ -683,7 +721,7 @@ __global__ void __launch_bounds__(128) k_rev_band16(PairSet ps, ResultSet rs, Sc
 #pragma unroll
         for (int k = 0; k < W; k++) cb[k] = cb[k + U];
 #pragma unroll
-        for (int k = W; k < NC; k++) cb[k] = code_at(i - G + k);
+        for (int k = W; k < NC; k++) cb[k] = code_at(i - L + k);
         a0 = n0;
         a1 = n1;
       }
