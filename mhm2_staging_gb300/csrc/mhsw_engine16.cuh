@@ -320,7 +320,8 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
     const int tm0 = 2 * G - 4, tm1 = N - 3;
     for (; t + 1 < T_end && t < tm0; t += 2) two_steps(std::true_type{});
     // eight steps per iteration in the middle phase (the loop's own instructions and the
-    // register moves at its back edge are paid once per eight steps)
+    // register moves at its back edge are paid once per eight steps); its last few steps
+    // go to the guarded drain loop, which keeps one copy of the step code fewer
     for (; t + 6 < tm1;) {
 #pragma unroll
       for (int u = 0; u < 4; u++) {
@@ -328,7 +329,6 @@ __device__ void sweep16_impl(const SeqView &A, const SeqView &B, const Scoring &
         t += 2;
       }
     }
-    for (; t < tm1; t += 2) two_steps(std::false_type{});
     for (; t + 1 < T_end; t += 2) two_steps(std::true_type{});
     if (t < T_end) {
       ST::load(tab, ceven, lane, Wlo, HA);
