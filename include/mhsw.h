@@ -269,11 +269,11 @@ int mhsw_align_pairs(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, i
  * another's work (klign overlaps its blocks the same way, src/klign.cpp:552-606): the
  * first enqueues the whole call -- copies in, kernels, the copy of out5 -- and returns;
  * mhsw_align_wait completes every call still pending (errors, timing, CIGAR rounds) and
- * must come before their out5 are read.  A handle keeps up to three host batches in
- * flight on three device input sets: a batch's copies wait only for the call three back,
- * so they run while earlier calls' kernels do (kernels stay in call order), and a copy the
- * host runs slowly is absorbed by the calls queued behind it; a fourth call first
- * completes the oldest.  Host arrays and out5 stay untouched by the caller until completed,
+ * must come before their out5 are read.  A handle keeps up to four host batches in
+ * flight on four device input sets (each reserved when first used): a batch's copies wait
+ * only for the call four back and for the previous call's copies, so they run while
+ * earlier calls' kernels do (kernels stay in call order), and a copy the host runs slowly
+ * is absorbed by the calls queued behind it; a fifth call first completes the oldest.  Host arrays and out5 stay untouched by the caller until completed,
  * and should be pinned for the copies to run asynchronously.  In score2 or CIGAR mode, for
  * device batches, and on any other call on the handle, pending calls complete first. */
 int mhsw_align_pairs_async(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form);

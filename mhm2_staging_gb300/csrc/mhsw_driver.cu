@@ -228,7 +228,7 @@ struct mhsw_driver {
   // copies run while earlier calls' kernels do, and a copy that runs slow (the host's copy
   // rate drops on some calls) is absorbed by the calls queued behind it; kernels stay in
   // order on the handle's stream.
-  static constexpr int kSlots = 3;
+  static constexpr int kSlots = 4;
   struct Pending {
     bool active = false;
     int64_t n = 0;

@@ -529,8 +529,9 @@ class GPUDriver:
         pt = pairs.c_struct()
         if hints:
             pt.max_a_len, pt.max_b_len, pt.cells, pt.a_bytes, pt.b_bytes = pairs.extents()
-        # the handle keeps up to three calls in flight: their arrays stay referenced here
-        self._pending = (list(getattr(self, "_pending", None) or []) + [(pairs, out, pt)])[-3:]
+        # the handle keeps up to four calls in flight (this call completes the one four back
+        # first): their arrays stay referenced here
+        self._pending = (list(getattr(self, "_pending", None) or []) + [(pairs, out, pt)])[-5:]
         self._ck(self._lib.mhsw_align_pairs_async(self._h, C.byref(pt), out.ctypes.data_as(_P) if n else None, 1,
                                                   form), "align_pairs_async")
         return out

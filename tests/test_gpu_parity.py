@@ -356,7 +356,7 @@ def test_async_halves_alternating_handles(built):
 
 
 def test_async_calls_in_flight_on_one_handle(built):
-    """Several host batches enqueued back to back on one handle (three in flight, the
+    """Several host batches enqueued back to back on one handle (four in flight, the
     copies of later ones overlapping earlier ones' kernels): every result matches the
     oracle."""
     batches = [workloads.generate(cfg, n=n, first=300 + k) for k, (cfg, n) in
