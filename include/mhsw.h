@@ -273,8 +273,9 @@ int mhsw_align_pairs(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, i
  * flight on four device input sets (each reserved when first used): a batch's copies wait
  * only for the call four back and for the previous call's copies, so they run while
  * earlier calls' kernels do (kernels stay in call order), and a copy the host runs slowly
- * is absorbed by the calls queued behind it; a fifth call first completes the oldest.  Host arrays and out5 stay untouched by the caller until completed,
- * and should be pinned for the copies to run asynchronously.  In score2 or CIGAR mode, for
+ * is absorbed by the calls queued behind it; a fifth call first completes the oldest.
+ * Host arrays and out5 stay untouched by the caller until completed, and should be pinned
+ * for the copies to run asynchronously.  In score2 or CIGAR mode, for
  * device batches, and on any other call on the handle, pending calls complete first. */
 int mhsw_align_pairs_async(mhsw_driver *drv, const mhsw_pairs *pairs, int32_t *out5, int host_io, int form);
 /* The records of the handle's last completed batch calls (at most 64 kept), oldest first:
@@ -286,7 +287,8 @@ int mhsw_last_tuning(mhsw_driver *drv, mhsw_tuning *out);
 /* Fixes the batched form's configuration and turns the tuner off: threads_per_block 64,
  * 128 or 256; blocks_per_sm 0 (occupancy limit) or a cap; lane_rows 128 or 160;
  * wide_try16 0 or 1 (mhsw_tuning).  threads_per_block 0 turns the tuner back on (the next
- * batched call re-tunes).  MHSW_ERR_ARG for other values. */
+ * batched call re-tunes; the configurations kept from earlier tunings are dropped).
+ * MHSW_ERR_ARG for other values. */
 int mhsw_driver_fix_batch_config(mhsw_driver *drv, int threads_per_block, int blocks_per_sm, int lane_rows,
                                  int wide_try16);
 int mhsw_align_wait(mhsw_driver *drv);

@@ -241,7 +241,7 @@ static bool within(double x, double y, double factor) {
 
 bool BatchSignature::close_to(const BatchSignature &o) const {
   if (max_a_class != o.max_a_class || !within(max_b, o.max_b, 2.0)) return false;
-  if (!(n < 65536 && o.n < 65536) && !within((double)n, (double)o.n, 8.0)) return false;
+  if (!(n <= 65536 && o.n <= 65536) && !within((double)n, (double)o.n, 8.0)) return false;
   if (a_mix[0] < 0 || o.a_mix[0] < 0) return true;  // a mix the host cannot see is not compared
   for (int c = 0; c < kSigClasses; c++)
     if (a_mix[c] - o.a_mix[c] > kTolerance || o.a_mix[c] - a_mix[c] > kTolerance) return false;
@@ -370,6 +370,18 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     return 0;
   };
 
+  // a configuration tuned earlier for a signature close to this one is taken back without
+  // trials (batches that alternate between workloads, such as full and partial serving
+  // micro-batches, tune once each)
+  if (bs.autotune && (!bs.tuned || !sig.close_to(bs.tuned_for))) {
+    for (int k = 0; k < bs.n_cached; k++)
+      if (sig.close_to(bs.cached[k].sig)) {
+        bs.shape = bs.cached[k].shape;
+        bs.tuned_for = bs.cached[k].sig;
+        bs.tuned = true;
+        break;
+      }
+  }
   if (bs.autotune && (!bs.tuned || !sig.close_to(bs.tuned_for))) {
     // Trials on a strided sample of the batch (every stride-th pair, so its length mix is
     // the batch's), sorted as the batch is.  Coordinate descent: the launch shape at the
@@ -448,6 +460,9 @@ int batched_forward(BatchState &bs, int device, const PairSet &ps, const ResultS
     bs.shape = best;
     bs.tuned_for = sig;
     bs.tuned = true;
+    bs.cached[bs.next_cached] = BatchState::Tuned{sig, best};
+    bs.next_cached = (bs.next_cached + 1) % BatchState::kCached;
+    if (bs.n_cached < BatchState::kCached) bs.n_cached++;
     tr.last_call_tuned = true;
     tr.wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
     bs.tune = tr;

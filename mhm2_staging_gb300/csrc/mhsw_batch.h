@@ -25,7 +25,7 @@ struct BatchShape {
 // device batch with size hints), the row class of its longest A, its longest B and its
 // size.  Two signatures describe the same workload when the longest A falls in the same
 // row class, the longest B within a factor of 2, the sizes within a factor of 8 (any two
-// below 65,536 pairs count as alike) and, where both mixes are known, no class fraction
+// of at most 65,536 pairs count as alike) and, where both mixes are known, no class fraction
 // moved by more than 0.15; ratios rather than fixed class edges keep batches that
 // straddle an edge (serving micro-batches of 1k..64k pairs) from re-tuning in turn.
 constexpr int kSigClasses = 8;
@@ -72,6 +72,15 @@ struct BatchState {
   BatchSignature tuned_for;
   bool tuned = false;
   bool autotune = true;
+  // the last kCached tuned configurations, taken back without trials for a batch whose
+  // signature is close to one of theirs
+  struct Tuned {
+    BatchSignature sig;
+    BatchShape shape;
+  };
+  static constexpr int kCached = 8;
+  Tuned cached[kCached];
+  int n_cached = 0, next_cached = 0;
   TuneRecord tune;
   void release();
 };
@@ -80,8 +89,9 @@ struct BatchState {
 // then descending B length), sorts the pair order on the device, and runs the
 // persistent kernel whose lane groups claim pairs from one atomic queue.  Pairs whose
 // score could exceed the int16 ceiling go straight to the int32 list wl.ovf.
-// A call whose batch signature differs from the one the handle last tuned for runs the
-// tuner first: timed trials of the persistent kernels on a strided sample of the batch
+// A call whose batch signature differs from the one the handle last tuned for takes back
+// the configuration of a close earlier signature (the last eight are kept), or else runs
+// the tuner first: timed trials of the persistent kernels on a strided sample of the batch
 // (at most 256k pairs) over the launch shape (groups per block, blocks per SM), the row
 // threshold between 8- and 16-lane groups (the rows each lane holds follow from it), and,
 // when the sample holds pairs whose score bound exceeds the int16 keys, their int16/int32

@@ -1662,6 +1662,7 @@ int mhsw_driver_fix_batch_config(mhsw_driver *d, int threads_per_block, int bloc
   if (threads_per_block == 0) {
     d->batch.autotune = true;
     d->batch.tuned = false;
+    d->batch.n_cached = d->batch.next_cached = 0;
     return MHSW_OK;
   }
   if ((threads_per_block != 64 && threads_per_block != 128 && threads_per_block != 256) || blocks_per_sm < 0 ||

@@ -60,6 +60,7 @@ struct Request {
   std::vector<int64_t> b_off;   // window offsets into the contig code arena
   std::vector<int32_t> b_len;
   std::vector<int64_t> wstart;  // window start within its contig
+  bool contiguous = true;       // each read starts where the previous one ends in src
   int32_t *out5 = nullptr;
   int64_t *win_start = nullptr;
   int32_t next = 0;       // first pair not yet on a slot
@@ -177,6 +178,24 @@ int mhsw_server::run_micro_batch(Slot *s, std::vector<Piece> &pieces, int64_t ro
   int64_t ab = 0;
   for (auto &pc : pieces) {
     Request &r = *pc.r;
+    if (r.contiguous) {
+      // the piece's reads are one run of the caller's buffer: one copy of the bytes, the
+      // per-pair fields as array copies
+      const int32_t f = pc.first;
+      const int64_t base = r.cum[(size_t)f];
+      std::memcpy(s->h_seq.p + ab, r.src + r.src_off[(size_t)f], (size_t)(r.cum[(size_t)f + pc.count] - base));
+      std::memcpy(s->h_alen.p + pc.row, r.len.data() + f, sizeof(int32_t) * (size_t)pc.count);
+      std::memcpy(s->h_boff.p + pc.row, r.b_off.data() + f, sizeof(int64_t) * (size_t)pc.count);
+      std::memcpy(s->h_blen.p + pc.row, r.b_len.data() + f, sizeof(int32_t) * (size_t)pc.count);
+      const int64_t shift = ab - base;
+      for (int32_t k = 0; k < pc.count; k++) {
+        s->h_aoff.p[pc.row + k] = r.cum[(size_t)f + k] + shift;
+        max_a = std::max(max_a, r.len[(size_t)f + k]);
+        max_b = std::max(max_b, r.b_len[(size_t)f + k]);
+      }
+      ab += r.cum[(size_t)f + pc.count] - base;
+      continue;
+    }
     for (int32_t k = 0; k < pc.count; k++) {
       const int32_t i = pc.first + k;
       const int64_t row = pc.row + k;
@@ -492,6 +511,7 @@ int mhsw_server_submit(mhsw_server *s, const mhsw_requests *req, int32_t *out5, 
     if (pos < 0 || pos >= cl) return s->fail(MHSW_ERR_ARG, "read %d: position %d outside contig %d", i, pos, cid);
     const int64_t ws = std::max<int64_t>(0, pos - flank), we = std::min<int64_t>(cl, pos + L + flank);
     if (we - ws > mhsw::kMaxB) return s->fail(MHSW_ERR_LIMIT, "read %d: window of %lld bases", i, (long long)(we - ws));
+    if (i > 0 && req->read_off[i] != req->read_off[i - 1] + req->read_len[i - 1]) r->contiguous = false;
     r->cum[(size_t)i] = total;
     r->len[(size_t)i] = L;
     r->b_off[(size_t)i] = s->coff[(size_t)cid] + ws;

@@ -55,6 +55,24 @@ def test_server_matches_oracle_on_uneven_batches(contigs, requests):
     srv.close()
 
 
+def test_reads_in_any_order_of_the_callers_buffer(contigs, requests):
+    """Request batches whose reads are not one run of the caller's buffer (a permuted
+    subset: each read packed on its own), and contiguous slices (packed as one run), mixed
+    in the same micro-batches: both match the oracle."""
+    srv = S.Server(slots=2, max_pairs_per_batch=3000)
+    srv.load_contigs(contigs)
+    rng = np.random.default_rng(11)
+    batches = [requests.subset(rng.permutation(np.arange(2000, 4500))), requests.slice(100, 1900),
+               requests.subset(np.arange(12000, 8000, -1)), requests.slice(20000, 21000)]
+    tickets = [srv.submit(b) for b in batches]
+    for b, t in zip(batches, tickets):
+        out5, ws = srv.wait(t)[:2]
+        want, wsw = _want(contigs, b)
+        assert not _diff(out5, want)
+        assert np.array_equal(ws, wsw)
+    srv.close()
+
+
 @pytest.mark.parametrize("form", [0, 1])
 def test_same_result_alone_and_in_the_mix(contigs, requests, form):
     probe = requests.slice(5000, 6500)

@@ -1,6 +1,7 @@
 """The batched form's tuner: a handle re-tunes when its batch's length signature moves
 (on a sample of the batch, within a bounded time), keeps its configuration while it does
-not, and every configuration it picks stays bit-exact against the oracle."""
+not, takes back the configuration of a signature it tuned for before, and every
+configuration it picks stays bit-exact against the oracle."""
 import numpy as np
 import pytest
 
@@ -33,6 +34,7 @@ def test_retunes_from_150_300_bp_pairs_to_the_uneven_workload(drv):
     t = _check(drv, p0)
     assert t["last_call_tuned"] == 1 and t["tunings"] == 1 and t["sample_pairs"] == 10_000
     assert t["trials"] >= 5 and len(t["trial_ms"]) == t["trials"]
+    shape0 = (t["threads_per_block"], t["blocks_per_sm"], t["lane_rows"], t["wide_try16"])
     t = _check(drv, p0)  # same workload: no tuning
     assert t["last_call_tuned"] == 0 and t["tunings"] == 1
     t = _check(drv, p2)  # new length mix and sizes: re-tuned on every second pair
@@ -42,8 +44,11 @@ def test_retunes_from_150_300_bp_pairs_to_the_uneven_workload(drv):
     assert t["lane_rows"] in (128, 160) and t["threads_per_block"] in (64, 128, 256)
     t = _check(drv, workloads.generate(2, n=300_000, first=300_000))  # same mix, other pairs
     assert t["last_call_tuned"] == 0 and t["tunings"] == 2
-    t = _check(drv, p0)  # back again
-    assert t["last_call_tuned"] == 1 and t["tunings"] == 3
+    t = _check(drv, p0)  # back again: the configuration tuned for it is taken back, no trials
+    assert t["last_call_tuned"] == 0 and t["tunings"] == 2
+    assert (t["threads_per_block"], t["blocks_per_sm"], t["lane_rows"], t["wide_try16"]) == shape0
+    t = _check(drv, p2)  # and forth
+    assert t["last_call_tuned"] == 0 and t["tunings"] == 2
 
 
 def _mix(seed: int, n: int, lo: int, hi: int, tail: int):
