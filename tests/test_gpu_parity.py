@@ -50,6 +50,21 @@ def test_config_samples(gpu, cfg, n, form):
     assert not _diff(got, want, pairs)
 
 
+@pytest.mark.parametrize("cfg,form", [(2, FORM_BATCHED), (1, FORM_PLAIN), (1, FORM_BATCHED), (4, FORM_BATCHED)])
+def test_whole_workloads_match_oracle(built, cfg, form):
+    """Whole workloads at their full sizes -- the benchmark's uneven batch (4M pairs,
+    3.34e11 cells), the 1M-pair read mix in both forms, the 200k long-reference pairs --
+    every pair against the oracle's vectorised form (bit-exact with the scalar one:
+    tests/test_oracle.py)."""
+    pairs = workloads.generate(cfg)
+    d = GPUDriver()
+    d.init(0, 1, 1, -3, -5, -2, 0)
+    d.set_ambiguity(-2)
+    got = d.align_pairs(pairs, form=form)
+    want = oracle.align_batch_lanes(pairs, SC)
+    assert not _diff(got, want, pairs)
+
+
 def test_dropin_protocol_klign(gpu):
     pairs = workloads.generate(1, n=3000)
     reads = [pairs.a(i) for i in range(pairs.n)]
