@@ -117,7 +117,7 @@ typedef struct {
  * since the handle's initialisation (no counterpart in the reference).  The kernels of a
  * call start once both its copies in have ended and the handle's stream has reached it
  * (the previous call's kernels are done); copies in wait only for their input set's call
- * two calls back. */
+ * four calls back and for the previous call's copies. */
 typedef struct {
   uint64_t seq;            /* call number on this handle */
   int64_t n_pairs;

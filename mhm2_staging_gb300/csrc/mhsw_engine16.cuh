@@ -2,7 +2,8 @@
 //
 // Same wavefront as sweep_pair in mhsw_engine.cuh (lane L holds rows [2KL, 2KL+2K) of a
 // strip, low halves at column j, high halves at column j-1, lane L two steps behind
-// lane L-1), with three changes that take work off the integer ALU pipe:
+// lane L-1), with these changes, which take work off the integer ALU pipe and out of the
+// issue slots:
 //
 //  1. Gap values are kept biased by the gap-open penalty: X^ = X + gO for X in {E, F}.
 //     Then X^' = max(X^ - gE, H) uses H directly, and
@@ -32,7 +33,13 @@
 //  4. B codes are read from global memory (each loaded two steps before its use) instead
 //     of being staged in shared memory, so a group's shared memory is its profile table only.
 //     The sweep runs in three phases: the middle one, where every lane's look-ahead column
-//     lies inside B, loads codes without the bounds test and the N substitution.
+//     lies inside B, loads codes without the bounds test and the N substitution, eight
+//     steps per loop iteration.
+//  5. A lane receives its left neighbour's last-row H and E^ words by two shuffles and
+//     takes their high halves with one byte permute each, whose selector is a per-lane
+//     register; lane 0 of a pair's first strip, whose row above is the zero boundary,
+//     holds a sign-replicate selector instead (H and E^ are never negative, so the
+//     replicated sign bytes are zero).
 //
 // Score2 mode (S2) also produces what SSW's second-best score is computed from
 // (ssw_core.cpp:489, :513-536): each A row's maximum of H, over B extended to P columns
