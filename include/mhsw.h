@@ -353,7 +353,9 @@ int mhsw_server_load_contigs(mhsw_server *s, const char *seq, const int64_t *off
 /* Admits a request batch once the queue budget has room; results go to out5
  * (5 * n int32: score, a_begin, a_end, b_begin, b_end, B coordinates relative to the
  * window) and win_start (n int64, may be NULL: contig offset of each window) when the
- * ticket completes; they and req->read_seq must stay valid until mhsw_server_wait returns. */
+ * ticket completes; they and req->read_seq must stay valid until mhsw_server_wait returns.
+ * A batch whose reads lie back to back in read_seq (each read_off the previous one's end)
+ * is packed for the device with one copy per micro-batch piece; others read by read. */
 int mhsw_server_submit(mhsw_server *s, const mhsw_requests *req, int32_t *out5, int64_t *win_start, int flags,
                        uint64_t *ticket);
 /* *done = 1 once the ticket's results are written. */
